@@ -1,0 +1,202 @@
+/* prestige_gpu.h -- C ABI of the GB300 (sm_103a) particle hot path.
+ *
+ * The reference (dineshadepu/prestige) describes a pairwise "equation" by the names of the
+ * particle slices it reads and writes: the #[equation] macro records them
+ * (prestige_macros/src/lib.rs:64-133) into EquationIR.reads / .writes
+ * (prestige/src/equations/ir.rs:3-14), fuse() merges equations
+ * (prestige/src/equations/fuse.rs:14-40), and the CPU backend runs the fused bodies as a gather
+ * into particle i over partners j (prestige/src/codegen/simple_cpu.rs:7-19).  The reference
+ * defines no FFI of its own.  This library keeps its contract -- particle data addressed by
+ * slice name, i = target, j = partner -- replaces the all-pairs j loop by a cell-list
+ * neighbour set, and keeps all state resident on one GPU.  Every entry point below is what a
+ * Rust `extern "C"` block (or ctypes) binds in place of the CPU loop; each comment names the
+ * reference interface it stands in for.
+ *
+ * Conventions
+ *   - Every call returns a pg_status; pg_last_error() gives a message for the calling thread.
+ *   - Host buffers are owned by the caller and only read/written during the call.
+ *   - A handle owns its device memory and one CUDA stream.  Calls on one handle must be
+ *     serialised by the caller; different handles are independent.
+ *   - Per-particle arrays cross the ABI in particle-id order (the order given to
+ *     pg_set_field).  Vector fields are interleaved (x0 y0 [z0] x1 y1 ...).
+ */
+#ifndef PRESTIGE_GPU_H
+#define PRESTIGE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PG_VERSION 1
+
+typedef enum pg_status {
+  PG_OK = 0,
+  PG_EINVAL = 1,    /* bad argument, size or configuration */
+  PG_ENOMEM = 2,    /* device allocation failed */
+  PG_EOVERFLOW = 3, /* a fixed capacity (contact slots, list capacity) was exceeded */
+  PG_ETIMEOUT = 4,  /* a bounded device wait gave up */
+  PG_ECUDA = 5,     /* CUDA runtime error (message in pg_last_error) */
+  PG_ESTATE = 6,    /* call not valid in the handle's current state */
+  PG_ENOTFOUND = 7  /* unknown field name */
+} pg_status;
+
+typedef enum pg_dtype { PG_F32 = 0, PG_F64 = 1, PG_U32 = 2 } pg_dtype;
+
+typedef enum pg_model { PG_MODEL_SPH = 0, PG_MODEL_DEM = 1 } pg_model;
+
+/* Pair-kernel arithmetic. */
+typedef enum pg_f64_mode {
+  PG_F64_NATIVE = 0, /* IEEE arithmetic in the system precision, oracle operation order (bit-exact) */
+  PG_F64_FAST = 1    /* f64 systems: double-word arithmetic on the FP32 pipe (f64 tolerance);
+                        f32 systems: fused multiply-add allowed */
+} pg_f64_mode;
+
+typedef struct pg_config {
+  int model;          /* pg_model */
+  int dim;            /* 2 or 3 (DEM: 3) */
+  int precision;      /* PG_F32 or PG_F64 (DEM: PG_F64) */
+  int gamma;          /* Tait exponent (integer, 1..15) */
+  long long n_fluid;  /* SPH: ids >= n_fluid (counted from the system's first id) are fixed
+                         dummy-wall particles; < 0 means all fluid */
+  double domain_lo[3], domain_hi[3]; /* cell-grid extent; particles outside are clamped into edge cells */
+  double cell_multiplier;            /* cell side = multiplier * support (1.0 or 0.5) */
+  /* SPH */
+  double h, rho0, c0, alpha, eps_av, tait_B; /* tait_B <= 0: B = rho0 c0^2 / gamma */
+  double gravity[3];
+  double dt;
+  /* DEM */
+  double kn, restitution, mu, kt, r_max;     /* kt <= 0: kt = 2/7 kn */
+  double wall_lo[3], wall_hi[3];
+  int contact_capacity;
+  /* tuning */
+  int block_size;     /* reserved (0) */
+  int f64_mode;       /* pg_f64_mode */
+  int reserved;
+} pg_config;
+
+/* Read-only description of a handle. */
+typedef struct pg_info {
+  long long n;        /* particles */
+  int n_systems, dim, precision, model, arith;
+  long long n_cells;  /* all systems */
+  int reach;          /* neighbour cells searched on each side */
+  int pass_grid;      /* blocks of the persistent pair pass */
+  int sort_passes;    /* 8-bit radix passes per step */
+  int graph;          /* 1 if steps replay a CUDA graph */
+  int grid_n[3];      /* system 0 */
+  double grid_lo[3];
+  double cell_size;
+} pg_info;
+
+/* Fill *cfg with defaults (3D f64 SPH, gamma 7, alpha 0.1, eps 0.01, multiplier 1). */
+void pg_config_default(pg_config* cfg);
+int pg_version(void);
+
+typedef struct pg_system pg_system;
+
+/* Create a system of n particles.  Stands in for the particle slices that a generated
+ * `for i in 0..n` loop indexes (prestige/src/codegen/simple_cpu.rs:7; n is unbound there). */
+int pg_create(const pg_config* cfg, size_t n, pg_system** out);
+
+/* One handle holding n_systems independent SPH systems, concatenated in id order:
+ * system s owns ids [sum_{t<s} counts[t], sum_{t<=s} counts[t]).  All systems share dim,
+ * precision, f64_mode and cell_multiplier.  No reference counterpart (the reference runs one
+ * loop over one set of slices); it batches many such loops into one launch. */
+int pg_batch_create(const pg_config* cfgs, const size_t* counts, int n_systems, pg_system** out);
+
+int pg_destroy(pg_system* sys);
+
+/* Copy a named slice between host and device.  Names are the slice identifiers an equation
+ * reads/writes (EquationIR.reads / .writes, prestige/src/equations/ir.rs:8-10):
+ *   SPH: "pos" (n*dim), "vel" (n*dim), "rho" (n), "mass" (n); read-only "acc" (n*dim) and
+ *        "drho" (n) after pg_compute_rates
+ *   DEM: "pos", "vel", "omega" (n*3), "radius" (n), "mass" (n)
+ *   any other name: a user scalar slice of n doubles, created by its first pg_set_field
+ *        (e.g. "force" of prestige/src/lib.rs:8).
+ * dtype PG_F64 or PG_F32 (converted to the stored precision). */
+int pg_set_field(pg_system* sys, const char* name, const void* host, size_t count, int dtype);
+int pg_get_field(pg_system* sys, const char* name, void* host, size_t count, int dtype);
+
+/* Neighbour search: cell hash, stable (cell, id) sort, cell-start table.  Replaces the all-pairs
+ * `for j in 0..n` of prestige/src/codegen/simple_cpu.rs:8. */
+int pg_build_neighbors(pg_system* sys);
+int pg_num_cells(pg_system* sys, size_t* n_cells);
+/* After pg_build_neighbors: per sorted slot k its cell and particle id; cell_start has
+ * n_cells + 1 entries (slots of cell c are cell_start[c] .. cell_start[c+1]). */
+int pg_get_neighbors(pg_system* sys, uint32_t* cell_sorted, uint32_t* ids_sorted, uint32_t* cell_start,
+                     size_t n_cells_plus_1);
+/* Number of neighbours (|x_i - x_j| < support, i itself included) of every particle, id order. */
+int pg_count_neighbors(pg_system* sys, uint32_t* counts);
+/* CSR neighbour lists in traversal order: offsets (n+1), neighbour ids (capacity entries).
+ * *total receives the entry count; PG_EOVERFLOW if it exceeds capacity. */
+int pg_get_neighbor_list(pg_system* sys, uint64_t* offsets, uint32_t* neighbors, size_t capacity, size_t* total);
+
+/* The body of the reference's eq1 (prestige/src/lib.rs:7-12, `force[i] += mass[j]`) run over
+ * the neighbour set instead of all j:  dst[i] += sum_{j : |x_i - x_j| < support} src[j]
+ * (j == i included).  dst and src name scalar double slices. */
+int pg_gather_sum(pg_system* sys, const char* dst, const char* src);
+
+/* SPH: evaluate the fused continuity + momentum rates without integrating ("acc" without
+ * gravity, "drho").  The GPU form of one generate_simple_cpu loop over the fused SPH equations
+ * (prestige/src/equations/fuse.rs:14-40, prestige/src/codegen/simple_cpu.rs:3-22). */
+int pg_compute_rates(pg_system* sys);
+
+/* Advance nsteps full steps (neighbour search + pair pass + integrator) and wait for them.
+ * pg_step_async only enqueues them on the handle's stream; pg_sync waits and reports
+ * device-side errors (PG_EOVERFLOW for DEM contact slots). */
+int pg_step(pg_system* sys, int nsteps);
+int pg_step_async(pg_system* sys, int nsteps);
+int pg_sync(pg_system* sys);
+
+/* Capture one full step as a CUDA graph; later steps replay it (same results). */
+int pg_enable_graph(pg_system* sys, int enable);
+
+/* DEM diagnostics: particle-particle contacts (both sides counted) in the last step. */
+int pg_dem_contacts(pg_system* sys, long long* contacts);
+/* DEM tangential history, id order: partner ids (n*capacity) and springs (n*capacity*3). */
+int pg_dem_get_history(pg_system* sys, uint32_t* partner, double* xi, size_t capacity);
+int pg_dem_set_history(pg_system* sys, const uint32_t* partner, const double* xi, size_t capacity);
+
+/* Differentiable SPH (f64, single system).  pg_forward_checkpointed runs nsteps from the current
+ * state, keeping the state every `every` steps.  pg_backward then takes dL/dx of the final
+ * positions (n*dim, id order) and returns dL/dalpha, dL/dB and dL/dv0 (n*dim, id order); any
+ * output pointer may be NULL.  The handle's state stays the final state.  No reference
+ * counterpart (the reference has no differentiation). */
+int pg_forward_checkpointed(pg_system* sys, int nsteps, int every);
+int pg_backward(pg_system* sys, const double* dL_dx, double* dL_dalpha, double* dL_dB, double* dL_dv0);
+
+/* Autotuner: time candidate (cell multiplier, arithmetic mode) settings on the handle's current
+ * state for `trial_steps` steps each, keep the fastest that meets the f64 tolerance, apply it and
+ * report it.  The handle's state is restored afterwards. */
+int pg_autotune(pg_system* sys, int trial_steps, int* best_block, double* best_multiplier, int* best_f64_mode,
+                double* best_ms_per_step);
+
+/* Device-side timing of steps (CUDA events on the handle's stream).  pg_timing_enable(1) resets
+ * the accumulators and makes every later step record events around its stages (steps then run
+ * eagerly, not from a graph); pg_timing_read waits for the stream and returns the totals since the
+ * last enable. */
+typedef struct pg_timing {
+  double region_ms;    /* first timed step start -> last timed step end */
+  double neighbor_ms;  /* hash + sort + cell table, summed over steps */
+  double gather_ms;    /* sorted copies, summed */
+  double pass_ms;      /* pair pass + integrator, summed */
+  long long steps;
+  long long launches;  /* kernels launched by the timed steps */
+} pg_timing;
+int pg_timing_enable(pg_system* sys, int enable);
+int pg_timing_read(pg_system* sys, pg_timing* out);
+
+int pg_memory_bytes(pg_system* sys, size_t* bytes);
+int pg_get_info(pg_system* sys, pg_info* info);
+
+/* Message for the last failing call on this thread ("" if none). */
+const char* pg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PRESTIGE_GPU_H */

@@ -1,0 +1,246 @@
+// DEM: linear spring-dashpot contacts (Cundall & Strack 1979) with a tangential history
+// spring capped by Coulomb friction, and the symplectic Euler integrator, in one pass.
+//
+// Like the SPH pass this is the reference's pairwise gather (prestige/src/lib.rs:7-12,
+// prestige/src/codegen/simple_cpu.rs:7-19) with j restricted to the neighbour cells:
+//   contact iff |x_ij|^2 < (r_i + r_j)^2;  n = x_ij/|x_ij|;  delta = r_i + r_j - |x_ij|
+//   vr = v_i - v_j - (r_i w_i + r_j w_j) x n;  vn = vr.n;  vt = vr - vn n
+//   fn = kn delta - gn vn,  gn = gcoef sqrt(m* kn),  gcoef = -2 ln e / sqrt(pi^2 + ln^2 e)
+//   xi = (xi_old - (xi_old.n) n) + vt dt;  ft = -kt xi - gn vt
+//   |ft| > mu |fn|:  ft <- mu|fn| ft/|ft|,  xi <- -(ft + gn vt)/kt
+//   F_i += fn n + ft;  T_i -= r_i n x ft
+// plus the six walls of the box (m* = m_i, no partner spin).  Each particle keeps up to
+// `capacity` history entries keyed by partner id (walls 0xFFFFFFF0 + face), in contact order.
+// All arithmetic is IEEE double in the oracle's operation order, so results are bit-exact.
+// Candidate counts are small (about 14 per sphere at config sizes) and contacts are rare,
+// so the pass is latency/memory bound rather than FP64 bound; no hit list is needed.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pg_internal.cuh"
+#include "pg_kernels.cuh"
+
+namespace pg {
+
+namespace {
+
+constexpr uint32_t kNoPartner = 0xFFFFFFFFu;
+constexpr uint32_t kWallId = 0xFFFFFFF0u;
+
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+__device__ __forceinline__ void cross3(const double* a, const double* b, double* c) {
+  c[0] = dsub(dmul(a[1], b[2]), dmul(a[2], b[1]));
+  c[1] = dsub(dmul(a[2], b[0]), dmul(a[0], b[2]));
+  c[2] = dsub(dmul(a[0], b[1]), dmul(a[1], b[0]));
+}
+
+struct Contact {
+  double nrm[3], delta, vr[3], meff, ri;
+};
+
+__device__ __forceinline__ void contact_law(const DemK& K, const Contact& ct, const double* xo, double* F, double* T,
+                                            double* xn) {
+  const double* n = ct.nrm;
+  const double vn = dadd(dadd(dmul(ct.vr[0], n[0]), dmul(ct.vr[1], n[1])), dmul(ct.vr[2], n[2]));
+  double vt[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) vt[c] = dsub(ct.vr[c], dmul(vn, n[c]));
+  const double gn = dmul(K.gcoef, __dsqrt_rn(dmul(ct.meff, K.kn)));
+  const double fn = dsub(dmul(K.kn, ct.delta), dmul(gn, vn));
+  const double xdn = dadd(dadd(dmul(xo[0], n[0]), dmul(xo[1], n[1])), dmul(xo[2], n[2]));
+  double xi[3], ft[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) xi[c] = dadd(dsub(xo[c], dmul(xdn, n[c])), dmul(vt[c], K.dt));
+#pragma unroll
+  for (int c = 0; c < 3; ++c) ft[c] = dsub(dmul(-K.kt, xi[c]), dmul(gn, vt[c]));
+  const double ft2 = dadd(dadd(dmul(ft[0], ft[0]), dmul(ft[1], ft[1])), dmul(ft[2], ft[2]));
+  const double lim = dmul(K.mu, fabs(fn));
+  if (ft2 > dmul(lim, lim)) {
+    const double scale = ddiv(lim, __dsqrt_rn(ft2));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      ft[c] = dmul(ft[c], scale);
+      xi[c] = ddiv(-dadd(ft[c], dmul(gn, vt[c])), K.kt);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) F[c] = dadd(F[c], dadd(dmul(fn, n[c]), ft[c]));
+  double nxf[3];
+  cross3(n, ft, nxf);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) T[c] = dsub(T[c], dmul(ct.ri, nxf[c]));
+#pragma unroll
+  for (int c = 0; c < 3; ++c) xn[c] = xi[c];
+}
+
+__global__ void dem_gather_kernel(DemArgs a) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.n) return;
+  const uint32_t id = a.sorted_id[k];
+  const size_t o = (size_t)id * 3;
+  a.sA[k] = make_double4_32a(a.pos[o], a.pos[o + 1], a.pos[o + 2], a.radius[id]);
+  a.sB[k] = make_double4_32a(a.vel[o], a.vel[o + 1], a.vel[o + 2], a.mass[id]);
+  a.sW[k] = make_double4_32a(a.omega[o], a.omega[o + 1], a.omega[o + 2], 0.0);
+}
+
+__global__ void __launch_bounds__(128) dem_pass_kernel(DemArgs a) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long my_contacts = 0;
+  if (k < a.n) {
+    const DemK& K = a.K[0];
+    const int C = K.capacity;
+    const uint32_t id = a.sorted_id[k];
+    const double4_32a Ai = a.sA[k], Bi = a.sB[k], Wi = a.sW[k];
+    const double xi[3] = {Ai.x, Ai.y, Ai.z};
+    const double vi[3] = {Bi.x, Bi.y, Bi.z};
+    const double wi[3] = {Wi.x, Wi.y, Wi.z};
+    const double ri = Ai.w, mi = Bi.w;
+    const uint32_t* hp_old = a.hpid_old + (size_t)id * C;
+    const double* hx_old = a.hxi_old + (size_t)id * C * 3;
+    uint32_t* hp_new = a.hpid_new + (size_t)id * C;
+    double* hx_new = a.hxi_new + (size_t)id * C * 3;
+    double F[3] = {0, 0, 0}, T[3] = {0, 0, 0};
+    int slot = 0;
+    bool overflow = false;
+
+    auto lookup = [&](uint32_t pid, double* out) {
+      out[0] = out[1] = out[2] = 0.0;
+      for (int s = 0; s < C; ++s) {
+        const uint32_t q = hp_old[s];
+        if (q == kNoPartner) break;
+        if (q == pid) {
+          out[0] = hx_old[s * 3];
+          out[1] = hx_old[s * 3 + 1];
+          out[2] = hx_old[s * 3 + 2];
+          break;
+        }
+      }
+    };
+    auto store = [&](uint32_t pid, const double* xv) {
+      if (slot < C) {
+        hp_new[slot] = pid;
+        hx_new[slot * 3] = xv[0];
+        hx_new[slot * 3 + 1] = xv[1];
+        hx_new[slot * 3 + 2] = xv[2];
+        ++slot;
+      } else {
+        overflow = true;
+      }
+    };
+
+    const GridK& g = K.g;
+    const uint32_t c = a.sorted_cell[k] - g.cell_base;
+    const int cx = (int)(c % (uint32_t)g.nx);
+    const int cy = (int)((c / (uint32_t)g.nx) % (uint32_t)g.ny);
+    const int cz = (int)(c / ((uint32_t)g.nx * (uint32_t)g.ny));
+    const int R = a.reach;
+    const int x0 = max(cx - R, 0), x1 = min(cx + R, g.nx - 1);
+    for (int dz = -R; dz <= R; ++dz) {
+      const int z = cz + dz;
+      if (z < 0 || z >= g.nz) continue;
+      for (int dy = -R; dy <= R; ++dy) {
+        const int y = cy + dy;
+        if (y < 0 || y >= g.ny) continue;
+        const uint32_t rb = g.cell_base + ((uint32_t)z * g.ny + (uint32_t)y) * g.nx;
+        const uint32_t s0 = a.cell_start[rb + x0], e0 = a.cell_start[rb + x1 + 1];
+        for (uint32_t t = s0; t < e0; ++t) {
+          const uint32_t j = a.sorted_id[t];
+          if (j == id) continue;
+          const double4_32a Aj = a.sA[t];
+          const double d[3] = {dsub(xi[0], Aj.x), dsub(xi[1], Aj.y), dsub(xi[2], Aj.z)};
+          const double d2 = dadd(dadd(dmul(d[0], d[0]), dmul(d[1], d[1])), dmul(d[2], d[2]));
+          const double rs = dadd(ri, Aj.w);
+          if (!(d2 < dmul(rs, rs))) continue;
+          const double4_32a Bj = a.sB[t], Wj = a.sW[t];
+          Contact ct;
+          const double dist = __dsqrt_rn(d2);
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) ct.nrm[cc] = ddiv(d[cc], dist);
+          ct.delta = dsub(rs, dist);
+          const double wj[3] = {Wj.x, Wj.y, Wj.z};
+          const double vj[3] = {Bj.x, Bj.y, Bj.z};
+          double ws[3], cr[3];
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) ws[cc] = dadd(dmul(ri, wi[cc]), dmul(Aj.w, wj[cc]));
+          cross3(ws, ct.nrm, cr);
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) ct.vr[cc] = dsub(dsub(vi[cc], vj[cc]), cr[cc]);
+          const double mj = Bj.w;
+          ct.meff = ddiv(dmul(mi, mj), dadd(mi, mj));
+          ct.ri = ri;
+          double xo[3], xn[3];
+          lookup(j, xo);
+          contact_law(K, ct, xo, F, T, xn);
+          store(j, xn);
+          ++my_contacts;
+        }
+      }
+    }
+    for (int face = 0; face < 6; ++face) {
+      const int ax = face / 2;
+      const bool hi_face = face & 1;
+      const double dist = hi_face ? dsub(K.wall_hi[ax], xi[ax]) : dsub(xi[ax], K.wall_lo[ax]);
+      if (!(dist < ri)) continue;
+      Contact ct;
+      ct.nrm[0] = ct.nrm[1] = ct.nrm[2] = 0.0;
+      ct.nrm[ax] = hi_face ? -1.0 : 1.0;
+      ct.delta = dsub(ri, dist);
+      double ws[3], cr[3];
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc) ws[cc] = dmul(ri, wi[cc]);
+      cross3(ws, ct.nrm, cr);
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc) ct.vr[cc] = dsub(vi[cc], cr[cc]);
+      ct.meff = mi;
+      ct.ri = ri;
+      double xo[3], xn[3];
+      lookup(kWallId + (uint32_t)face, xo);
+      contact_law(K, ct, xo, F, T, xn);
+      store(kWallId + (uint32_t)face, xn);
+    }
+    for (int s = slot; s < C; ++s) {
+      hp_new[s] = kNoPartner;
+      hx_new[s * 3] = 0.0;
+      hx_new[s * 3 + 1] = 0.0;
+      hx_new[s * 3 + 2] = 0.0;
+    }
+    if (overflow) atomicOr(a.err, ERR_CONTACT_OVERFLOW);
+
+    // symplectic Euler: v' = v + dt (F/m + g); x' = x + dt v'; w' = w + dt T / (0.4 m r^2)
+    const double I = dmul(dmul(dmul(0.4, mi), ri), ri);
+    const size_t o = (size_t)id * 3;
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) {
+      const double v = dadd(vi[cc], dmul(K.dt, dadd(ddiv(F[cc], mi), K.grav[cc])));
+      a.vel[o + cc] = v;
+      a.pos[o + cc] = dadd(xi[cc], dmul(K.dt, v));
+      a.omega[o + cc] = dadd(wi[cc], dmul(K.dt, ddiv(T[cc], I)));
+    }
+  }
+  // contact count: warp sum, one atomic per warp
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) my_contacts += __shfl_down_sync(0xffffffffu, my_contacts, off);
+  if ((threadIdx.x & 31) == 0 && my_contacts) atomicAdd(a.contacts, my_contacts);
+}
+
+}  // namespace
+
+int launch_dem_gather(cudaStream_t st, const DemArgs& a) {
+  if (a.n == 0) return PG_OK;
+  dem_gather_kernel<<<(a.n + 255) / 256, 256, 0, st>>>(a);
+  PG_CUDA_TRY(cudaGetLastError());
+  return PG_OK;
+}
+
+int launch_dem_pass(cudaStream_t st, const DemArgs& a) {
+  if (a.n == 0) return PG_OK;
+  dem_pass_kernel<<<(a.n + 127) / 128, 128, 0, st>>>(a);
+  PG_CUDA_TRY(cudaGetLastError());
+  return PG_OK;
+}
+
+}  // namespace pg

@@ -1,0 +1,123 @@
+// Kernel-ready parameter records and launchers shared by the .cu files of the library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pg_internal.cuh"
+
+namespace pg {
+
+// Arithmetic of the pair kernels.
+enum Arith {
+  ARITH_F64_EXACT = 0,  // IEEE double, oracle operation order (bit-exact)
+  ARITH_F64_DF = 1,     // double-word arithmetic on the FP32 pipe (f64 tolerance)
+  ARITH_F32_EXACT = 2,  // IEEE single, oracle operation order (bit-exact)
+  ARITH_F32_FAST = 3,   // single precision with fused multiply-add
+};
+
+constexpr int kSphThreads = 128;
+
+// SPH constants of one system in one precision (formulas of the oracle's sph_consts).
+template <class R>
+struct SphC {
+  R fa, fb, inv_h, four_h2, avk, eps_h2, B, inv_rho0, dt;
+  R g[3];
+};
+
+// Double-word (hi, lo) copies of the constants for the f64 fast mode.
+struct SphDF {
+  float fa[2], fb[2], inv_h[2], four_h2[2], avk[2], eps_h2[2];
+  float band;  // |r^2 - (2h)^2| below which the exact f64 test decides
+};
+
+struct SphK {
+  GridK g;
+  SphC<double> d;
+  SphC<float> f;
+  SphDF w;
+  float two_h_f;
+  uint32_t id_begin, id_end, fluid_end;  // global ids; ids >= fluid_end are fixed wall particles
+  int gamma;
+};
+
+struct SphArgs {
+  const SphK* sys;           // per system (device)
+  const uint32_t* sys_of_id; // null for a single system
+  uint32_t n;
+  int dim, reach;
+  const uint32_t* sorted_cell;
+  const uint32_t* sorted_id;
+  const uint32_t* cell_start;
+  void* s[6];                // sorted packed arrays (layout per arithmetic mode)
+  void* pos;                 // canonical state, id order
+  void* vel;
+  void* rho;
+  void* mass;
+  void* acc;                 // optional rates output, id order
+  void* drho;
+  int integrate;
+};
+
+int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith);
+int launch_sph_pass(cudaStream_t st, const SphArgs& a, int arith, int grid);
+int sph_pass_occupancy(int arith, int dim);
+// Bytes per particle of the sorted packed arrays s[0..5] for an arithmetic mode.
+void sph_sorted_layout(int arith, size_t sizes[6]);
+
+// ---------------------------------------------------------------------------------------
+// Neighbour utilities (counts, CSR lists, the eq1 gather) on the sorted positions.
+// ---------------------------------------------------------------------------------------
+struct NbrArgs {
+  const GridK* grid;          // per system (device)
+  const uint32_t* sys_of_id;  // null for a single system
+  uint32_t n;
+  int dim, reach, f64;
+  const uint32_t* sorted_cell;
+  const uint32_t* sorted_id;
+  const uint32_t* cell_start;
+  const void* spos;           // sorted positions: double4_32a or float4 (x, y, z, 0)
+};
+
+int launch_sorted_positions(cudaStream_t st, const NbrArgs& a, const void* pos, void* spos);
+int launch_neighbor_counts(cudaStream_t st, const NbrArgs& a, uint32_t* counts_by_id);
+int launch_neighbor_list(cudaStream_t st, const NbrArgs& a, const uint32_t* offs_by_id, uint32_t* nbr);
+int launch_gather_sum(cudaStream_t st, const NbrArgs& a, const double* src_sorted, double* dst_by_id);
+int launch_gather_field(cudaStream_t st, const uint32_t* sorted_id, uint32_t n, const double* src, double* out);
+
+// ---------------------------------------------------------------------------------------
+// DEM.
+// ---------------------------------------------------------------------------------------
+struct DemK {
+  GridK g;
+  double kn, kt, mu, dt, gcoef;
+  double grav[3], wall_lo[3], wall_hi[3];
+  int capacity;
+};
+
+struct DemArgs {
+  const DemK* K;  // device
+  uint32_t n;
+  int reach;
+  const uint32_t* sorted_cell;
+  const uint32_t* sorted_id;
+  const uint32_t* cell_start;
+  double4_32a* sA;  // x, y, z, r
+  double4_32a* sB;  // vx, vy, vz, m
+  double4_32a* sW;  // wx, wy, wz, 0
+  double* pos;
+  double* vel;
+  double* omega;
+  const double* radius;
+  const double* mass;
+  const uint32_t* hpid_old;
+  const double* hxi_old;
+  uint32_t* hpid_new;
+  double* hxi_new;
+  unsigned long long* contacts;
+  unsigned* err;
+};
+
+int launch_dem_gather(cudaStream_t st, const DemArgs& a);
+int launch_dem_pass(cudaStream_t st, const DemArgs& a);
+
+}  // namespace pg

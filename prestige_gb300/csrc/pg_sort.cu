@@ -1,0 +1,296 @@
+// Neighbour-search integer stages: device exclusive scan, stable LSD radix sort of
+// (cell, particle id) pairs, and the cell-start table.
+//
+// The reference executes an equation as `for i in 0..n { for j in 0..n { body } }`
+// (prestige/src/codegen/simple_cpu.rs:7-8).  These stages replace the inner all-pairs loop
+// by a cell list: particles are ordered by (cell, id) and cell c owns the slots
+// cell_start[c] .. cell_start[c+1].  Everything here is integer work and bit-exact against
+// the oracle's stable counting sort.
+//
+// Sort: 8-bit digits, least significant first.  Each pass is three launches:
+//   digit_hist   per tile of 4096 keys, a 256-bin histogram          -> hist[d * tiles + t]
+//   digit_scan   per digit, exclusive scan over tiles (in place)    -> digit_total[d]
+//   digit_scatter stable per-tile ranking with warp match masks, then scatter
+// Input order is id order, and every pass is stable, so equal cells stay in id order.
+#include <cuda_runtime.h>
+
+#include "pg_internal.cuh"
+
+namespace pg {
+
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys per tile
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kWarpChunk = kSortTile / kSortWarps;    // 512 consecutive keys per warp
+constexpr int kRadix = 256;
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;  // 4096 values per block
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+// Block-wide exclusive scan of one value per thread (blockDim.x multiple of 32, <= 1024).
+// Returns the exclusive prefix; *total receives the block sum.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t warp_sums[32];
+  __shared__ uint32_t block_total;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  uint32_t incl = warp_incl_scan(v);
+  if (lane == 31) warp_sums[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t s = lane < nwarps ? warp_sums[lane] : 0u;
+    uint32_t si = warp_incl_scan(s);
+    if (lane < nwarps) warp_sums[lane] = si - s;
+    if (lane == nwarps - 1) block_total = si;
+  }
+  __syncthreads();
+  uint32_t r = incl - v + warp_sums[warp];
+  if (total) *total = block_total;
+  __syncthreads();
+  return r;
+}
+
+// ---------------------------------------------------------------------------------------
+// Exclusive scan (reduce, scan block sums, rescan).  out[m] receives the total.
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const uint32_t* __restrict__ in, size_t m,
+                                                                   uint32_t* __restrict__ bsum) {
+  const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k)
+    if (base + k < m) s += in[base + k];
+  uint32_t total;
+  block_excl_scan(s, &total);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+// One block scans the block sums sequentially in chunks of kScanThreads (any count).
+__global__ void __launch_bounds__(kScanThreads) scan_bsum_kernel(uint32_t* __restrict__ bsum, size_t nb) {
+  uint32_t carry = 0;
+  for (size_t c0 = 0; c0 < nb; c0 += kScanThreads) {
+    const size_t i = c0 + threadIdx.x;
+    uint32_t v = i < nb ? bsum[i] : 0u;
+    uint32_t total;
+    uint32_t ex = block_excl_scan(v, &total);
+    if (i < nb) bsum[i] = ex + carry;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const uint32_t* __restrict__ in, size_t m,
+                                                                  const uint32_t* __restrict__ bsum,
+                                                                  uint32_t* __restrict__ out) {
+  const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = base + k < m ? in[base + k] : 0u;
+    s += v[k];
+  }
+  uint32_t total;
+  uint32_t ex = block_excl_scan(s, &total) + bsum[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < m) out[base + k] = ex;
+    ex += v[k];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[m] = bsum[blockIdx.x] + total;
+}
+
+// ---------------------------------------------------------------------------------------
+// Radix sort passes.
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kSortThreads) digit_hist_kernel(const uint32_t* __restrict__ keys, size_t n,
+                                                                  int shift, int tiles,
+                                                                  uint32_t* __restrict__ hist) {
+  __shared__ uint32_t cnt[kRadix];
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const size_t base = (size_t)blockIdx.x * kSortTile;
+#pragma unroll 4
+  for (int it = 0; it < kSortItems; ++it) {
+    const size_t i = base + (size_t)it * kSortThreads + threadIdx.x;
+    if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 0xffu], 1u);
+  }
+  __syncthreads();
+  hist[(size_t)threadIdx.x * tiles + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// Block d: exclusive scan of hist[d * tiles .. + tiles) in place; total -> digit_total[d].
+__global__ void __launch_bounds__(kSortThreads) digit_scan_kernel(uint32_t* __restrict__ hist, int tiles,
+                                                                  uint32_t* __restrict__ digit_total) {
+  uint32_t* row = hist + (size_t)blockIdx.x * tiles;
+  uint32_t carry = 0;
+  for (int c0 = 0; c0 < tiles; c0 += kSortThreads) {
+    const int i = c0 + threadIdx.x;
+    uint32_t v = i < tiles ? row[i] : 0u;
+    uint32_t total;
+    uint32_t ex = block_excl_scan(v, &total);
+    if (i < tiles) row[i] = ex + carry;
+    carry += total;
+  }
+  if (threadIdx.x == 0) digit_total[blockIdx.x] = carry;
+}
+
+// Stable scatter of one tile.  Warp w owns keys [base + w*512, base + (w+1)*512) and walks
+// them in 16 rounds of 32; within a round, lanes with equal digits are ranked by lane
+// (match mask), and a per-warp running count per digit carries the rank across rounds.
+// Warps are then ordered by an exclusive scan of the per-warp counts per digit.
+__global__ void __launch_bounds__(kSortThreads) digit_scatter_kernel(
+    const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ keys_out,
+    uint32_t* __restrict__ vals_out, size_t n, int shift, int tiles, const uint32_t* __restrict__ hist,
+    const uint32_t* __restrict__ digit_total) {
+  __shared__ uint32_t wcnt[kSortWarps][kRadix];
+  __shared__ uint32_t tile_off[kRadix];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // global offset of digit d in this tile = (sum of smaller digits) + (this digit in earlier tiles)
+  {
+    uint32_t total;
+    uint32_t dbase = block_excl_scan(digit_total[tid], &total);
+    tile_off[tid] = dbase + hist[(size_t)tid * tiles + blockIdx.x];
+  }
+#pragma unroll
+  for (int w = 0; w < kSortWarps; ++w) wcnt[w][tid] = 0;
+  __syncthreads();
+
+  const size_t base = (size_t)blockIdx.x * kSortTile + (size_t)warp * kWarpChunk;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const size_t i = base + (size_t)r * 32 + lane;
+    const bool valid = i < n;
+    key[r] = valid ? keys_in[i] : 0u;
+    val[r] = valid ? vals_in[i] : 0u;
+    const uint32_t dkey = valid ? ((key[r] >> shift) & 0xffu) : 0x100u;
+    const uint32_t peers = __match_any_sync(0xffffffffu, dkey);
+    const int leader = __ffs(peers) - 1;
+    uint32_t old = 0;
+    if (valid && lane == leader) {
+      old = wcnt[warp][dkey];
+      wcnt[warp][dkey] = old + __popc(peers);
+    }
+    old = __shfl_sync(0xffffffffu, old, leader);
+    rank[r] = old + __popc(peers & lt_mask);
+    __syncwarp();
+  }
+  __syncthreads();
+  {  // per digit: exclusive scan over warps
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) {
+      const uint32_t t = wcnt[w][tid];
+      wcnt[w][tid] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const size_t i = base + (size_t)r * 32 + lane;
+    if (i < n) {
+      const uint32_t d = (key[r] >> shift) & 0xffu;
+      const uint32_t pos = tile_off[d] + wcnt[warp][d] + rank[r];
+      keys_out[pos] = key[r];
+      vals_out[pos] = val[r];
+    }
+  }
+}
+
+// cell_count[c] = number of particles in cell c (integer atomics: the result is exact).
+__global__ void cell_count_kernel(const uint32_t* __restrict__ cell, size_t n, uint32_t* __restrict__ cnt) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) atomicAdd(&cnt[cell[i]], 1u);
+}
+
+int bits_needed(uint64_t v) {
+  int b = 0;
+  while (v) {
+    ++b;
+    v >>= 1;
+  }
+  return b;
+}
+
+}  // namespace
+
+size_t scan_tmp_words(size_t m) { return (m + kScanTile - 1) / kScanTile + 1; }
+
+int launch_exclusive_scan(cudaStream_t st, const uint32_t* in, uint32_t* out, size_t m, uint32_t* tmp) {
+  if (m == 0) {
+    PG_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(uint32_t), st));
+    return PG_OK;
+  }
+  const size_t nb = (m + kScanTile - 1) / kScanTile;
+  scan_reduce_kernel<<<(unsigned)nb, kScanThreads, 0, st>>>(in, m, tmp);
+  scan_bsum_kernel<<<1, kScanThreads, 0, st>>>(tmp, nb);
+  scan_apply_kernel<<<(unsigned)nb, kScanThreads, 0, st>>>(in, m, tmp, out);
+  PG_CUDA_TRY(cudaGetLastError());
+  return PG_OK;
+}
+
+int NbrWork::init(size_t n_, uint64_t ncells_) {
+  n = n_;
+  ncells = ncells_;
+  const int bits = bits_needed(ncells ? ncells - 1 : 0);
+  passes = (bits + 7) / 8;
+  tiles = (int)((n + kSortTile - 1) / kSortTile);
+  if (tiles < 1) tiles = 1;
+  const size_t nn = n ? n : 1;
+  PG_TRY(keys[0].ensure(nn * 4));
+  PG_TRY(keys[1].ensure(nn * 4));
+  PG_TRY(vals[0].ensure(nn * 4));
+  PG_TRY(vals[1].ensure(nn * 4));
+  PG_TRY(hist.ensure((size_t)kRadix * tiles * 4));
+  PG_TRY(digit_total.ensure(kRadix * 4));
+  PG_TRY(cell_count.ensure((ncells ? ncells : 1) * 4));
+  PG_TRY(cell_start.ensure((ncells + 1) * 4));
+  PG_TRY(scan_tmp.ensure(scan_tmp_words(ncells) * 4));
+  return PG_OK;
+}
+
+size_t NbrWork::bytes() const {
+  return keys[0].bytes + keys[1].bytes + vals[0].bytes + vals[1].bytes + hist.bytes + digit_total.bytes +
+         cell_count.bytes + cell_start.bytes + scan_tmp.bytes;
+}
+
+int sort_and_table(cudaStream_t st, NbrWork& w) {
+  const size_t n = w.n;
+  int cur = 0;
+  for (int p = 0; p < w.passes; ++p) {
+    const int shift = 8 * p;
+    digit_hist_kernel<<<w.tiles, kSortThreads, 0, st>>>(w.keys[cur].as<uint32_t>(), n, shift, w.tiles,
+                                                        w.hist.as<uint32_t>());
+    digit_scan_kernel<<<kRadix, kSortThreads, 0, st>>>(w.hist.as<uint32_t>(), w.tiles, w.digit_total.as<uint32_t>());
+    digit_scatter_kernel<<<w.tiles, kSortThreads, 0, st>>>(
+        w.keys[cur].as<uint32_t>(), w.vals[cur].as<uint32_t>(), w.keys[cur ^ 1].as<uint32_t>(),
+        w.vals[cur ^ 1].as<uint32_t>(), n, shift, w.tiles, w.hist.as<uint32_t>(), w.digit_total.as<uint32_t>());
+    cur ^= 1;
+  }
+  w.sorted_cell = w.keys[cur].as<uint32_t>();
+  w.sorted_id = w.vals[cur].as<uint32_t>();
+  // cell table: count per cell, exclusive scan -> start (start[ncells] = n)
+  PG_CUDA_TRY(cudaMemsetAsync(w.cell_count.p, 0, w.ncells * 4, st));
+  if (n) cell_count_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(w.sorted_cell, n, w.cell_count.as<uint32_t>());
+  PG_TRY(launch_exclusive_scan(st, w.cell_count.as<uint32_t>(), w.cell_start.as<uint32_t>(), w.ncells,
+                               w.scan_tmp.as<uint32_t>()));
+  PG_CUDA_TRY(cudaGetLastError());
+  return PG_OK;
+}
+
+}  // namespace pg

@@ -1,0 +1,546 @@
+// Weakly-compressible SPH on the cell list: continuity, Tait pressure, Monaghan artificial
+// viscosity and the kick-drift integrator, fused into one pass per step.
+//
+// The reference states a pairwise equation as a gather into particle i over partners j
+// (prestige/src/lib.rs:7-12 `force[i] += mass[j]`, executed by the loop of
+// prestige/src/codegen/simple_cpu.rs:7-19).  This pass is that gather for the SPH rates,
+// with j restricted to the particles of the neighbour cells and r_ij < 2h:
+//   drho_i = sum_j m_j (v_ij . x_ij) F_ij
+//   a_i    = -sum_j m_j (P_i + P_j + Pi_ij) F_ij x_ij            (+ g in the integrator)
+//   F = (dW/dr)/r of the cubic spline (support 2h), P = p/rho^2, p = B((rho/rho0)^gamma - 1)
+//   Pi_ij  = -2 alpha c0 h (v_ij.x_ij) / ((r^2 + eps h^2)(rho_i + rho_j))  if v_ij.x_ij < 0
+//
+// Kernel structure (one thread per target particle i, slot order):
+//   phase 1  every candidate of the 9 (2D: 3) neighbour rows is tested in FP32 against a
+//            conservative bound on r^2; passing slots are appended to a per-thread list in
+//            shared memory.  Lanes walk their own concatenated candidate sequence, so a warp
+//            loops max_lane(candidates) times rather than sum_rows(max_lane(row length)).
+//   phase 2  when any lane's list is full (or all lanes are done) the warp evaluates the
+//            listed pairs: the exact neighbour test, then the pair terms.  Nearly all lanes
+//            are busy, instead of ~15% of them under a per-candidate branch.
+// Pairs are evaluated in the oracle's order (rows z, y ascending; slots ascending), so the
+// IEEE modes reproduce the oracle bit for bit.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pg_arith.cuh"
+#include "pg_internal.cuh"
+#include "pg_kernels.cuh"
+
+namespace pg {
+
+namespace {
+
+constexpr int kHitCap = 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+template <class R> struct V4;
+template <> struct V4<double> { typedef double4_32a T; };
+template <> struct V4<float> { typedef float4 T; };
+
+template <class R> __device__ __forceinline__ const SphC<R>& consts(const SphK& K);
+template <> __device__ __forceinline__ const SphC<double>& consts<double>(const SphK& K) { return K.d; }
+template <> __device__ __forceinline__ const SphC<float>& consts<float>(const SphK& K) { return K.f; }
+
+// p / rho^2 with p = B((rho/rho0)^gamma - 1), operation order of the oracle's tait_pterm.
+template <class Ops>
+__device__ __forceinline__ typename Ops::R tait_pterm(const SphC<typename Ops::R>& c, int gamma,
+                                                      typename Ops::R rho) {
+  typedef typename Ops::R R;
+  const R rr = Ops::mul(rho, c.inv_rho0);
+  R pw = rr;
+  for (int e = 1; e < gamma; ++e) pw = Ops::mul(pw, rr);
+  const R p = Ops::mul(c.B, Ops::sub(pw, R(1)));
+  return Ops::div(p, Ops::mul(rho, rho));
+}
+
+__device__ __forceinline__ uint32_t sys_of_slot(const SphArgs& a, uint32_t id) {
+  return a.sys_of_id ? a.sys_of_id[id] : 0u;
+}
+
+// ---------------------------------------------------------------------------------------
+// Sorted gather: slot k <- particle sorted_id[k]; precomputes P = p / rho^2.
+// ---------------------------------------------------------------------------------------
+template <class Ops, int DIM>
+__global__ void sph_gather_real(SphArgs a) {
+  typedef typename Ops::R R;
+  typedef typename V4<R>::T R4;
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.n) return;
+  const uint32_t id = a.sorted_id[k];
+  const SphK& K = a.sys[sys_of_slot(a, id)];
+  const R* pos = (const R*)a.pos;
+  const R* vel = (const R*)a.vel;
+  const R rho = ((const R*)a.rho)[id];
+  const R m = ((const R*)a.mass)[id];
+  R x[3] = {0, 0, 0}, v[3] = {0, 0, 0};
+#pragma unroll
+  for (int c = 0; c < DIM; ++c) {
+    x[c] = pos[(size_t)id * DIM + c];
+    v[c] = vel[(size_t)id * DIM + c];
+  }
+  R4 A, B;
+  A.x = x[0]; A.y = x[1]; A.z = x[2]; A.w = m;
+  B.x = v[0]; B.y = v[1]; B.z = v[2]; B.w = rho;
+  ((R4*)a.s[0])[k] = A;
+  ((R4*)a.s[1])[k] = B;
+  ((R*)a.s[2])[k] = tait_pterm<Ops>(consts<R>(K), K.gamma, rho);
+  if (sizeof(R) == 8) ((float4*)a.s[3])[k] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
+}
+
+// Double-word copies for the f64 fast mode:
+//   s0 {x,y,z,m}.hi  s1 {x,y,z,m}.lo  s2 {vx,vy,vz,P}.hi  s3 {vx,vy,vz,P}.lo  s4 rho (hi,lo)
+//   s5 double {x,y,z} for the exact neighbour test near the cut-off.
+template <int DIM>
+__global__ void sph_gather_df(SphArgs a) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.n) return;
+  const uint32_t id = a.sorted_id[k];
+  const SphK& K = a.sys[sys_of_slot(a, id)];
+  const double* pos = (const double*)a.pos;
+  const double* vel = (const double*)a.vel;
+  const double rho = ((const double*)a.rho)[id];
+  const double m = ((const double*)a.mass)[id];
+  double x[3] = {0, 0, 0}, v[3] = {0, 0, 0};
+#pragma unroll
+  for (int c = 0; c < DIM; ++c) {
+    x[c] = pos[(size_t)id * DIM + c];
+    v[c] = vel[(size_t)id * DIM + c];
+  }
+  const double P = tait_pterm<OpsD>(K.d, K.gamma, rho);
+  float4 ah, al, bh, bl;
+  df_split(x[0], &ah.x, &al.x);
+  df_split(x[1], &ah.y, &al.y);
+  df_split(x[2], &ah.z, &al.z);
+  df_split(m, &ah.w, &al.w);
+  df_split(v[0], &bh.x, &bl.x);
+  df_split(v[1], &bh.y, &bl.y);
+  df_split(v[2], &bh.z, &bl.z);
+  df_split(P, &bh.w, &bl.w);
+  float2 r;
+  df_split(rho, &r.x, &r.y);
+  ((float4*)a.s[0])[k] = ah;
+  ((float4*)a.s[1])[k] = al;
+  ((float4*)a.s[2])[k] = bh;
+  ((float4*)a.s[3])[k] = bl;
+  ((float2*)a.s[4])[k] = r;
+  ((double4_32a*)a.s[5])[k] = make_double4_32a(x[0], x[1], x[2], 0.0);
+}
+
+// ---------------------------------------------------------------------------------------
+// Pair-term policies.
+// ---------------------------------------------------------------------------------------
+template <class Ops, int DIM, bool EXACT_TEST>
+struct RealPairs {
+  typedef typename Ops::R R;
+  typedef typename V4<R>::T R4;
+  const R4* A;
+  const R4* B;
+  const R* P;
+  SphC<R> c;
+  R xi[3], vi[3], rhoi, Pi;
+  R acc[3], dr;
+
+  __device__ __forceinline__ void begin(const SphArgs& a, const SphK& K, uint32_t k) {
+    A = (const R4*)a.s[0];
+    B = (const R4*)a.s[1];
+    P = (const R*)a.s[2];
+    c = consts<R>(K);
+    const R4 Ai = A[k], Bi = B[k];
+    xi[0] = Ai.x; xi[1] = Ai.y; xi[2] = Ai.z;
+    vi[0] = Bi.x; vi[1] = Bi.y; vi[2] = Bi.z;
+    rhoi = Bi.w;
+    Pi = P[k];
+    acc[0] = acc[1] = acc[2] = R(0);
+    dr = R(0);
+  }
+
+  __device__ __forceinline__ void pair(uint32_t t) {
+    const R4 Aj = A[t];
+    const R d0 = Ops::sub(xi[0], Aj.x), d1 = Ops::sub(xi[1], Aj.y);
+    const R d2 = DIM == 3 ? Ops::sub(xi[2], Aj.z) : R(0);
+    R r2 = Ops::add(Ops::mul(d0, d0), Ops::mul(d1, d1));
+    if (DIM == 3) r2 = Ops::add(r2, Ops::mul(d2, d2));
+    if (EXACT_TEST) {
+      if (!(r2 < c.four_h2)) return;
+      if (!(r2 > R(0))) return;
+    }
+    const R4 Bj = B[t];
+    const R Pj = P[t];
+    const R r = Ops::sqrt(r2);
+    const R q = Ops::mul(r, c.inv_h);
+    R F;
+    if (q < R(1)) {
+      F = Ops::mul(c.fa, Ops::sub(Ops::mul(R(2.25), q), R(3)));
+    } else {
+      const R tq = Ops::sub(R(2), q);
+      F = Ops::div(Ops::mul(c.fb, Ops::mul(tq, tq)), r);
+    }
+    const R dv0 = Ops::sub(vi[0], Bj.x), dv1 = Ops::sub(vi[1], Bj.y);
+    const R dv2 = DIM == 3 ? Ops::sub(vi[2], Bj.z) : R(0);
+    R w = Ops::add(Ops::mul(dv0, d0), Ops::mul(dv1, d1));
+    if (DIM == 3) w = Ops::add(w, Ops::mul(dv2, d2));
+    const R mj = Aj.w;
+    dr = Ops::add(dr, Ops::mul(mj, Ops::mul(w, F)));
+    R pij = R(0);
+    if (w < R(0)) pij = Ops::div(Ops::mul(c.avk, w), Ops::mul(Ops::add(r2, c.eps_h2), Ops::add(rhoi, Bj.w)));
+    const R coef = Ops::mul(mj, Ops::mul(Ops::add(Ops::add(Pi, Pj), pij), F));
+    acc[0] = Ops::sub(acc[0], Ops::mul(coef, d0));
+    acc[1] = Ops::sub(acc[1], Ops::mul(coef, d1));
+    if (DIM == 3) acc[2] = Ops::sub(acc[2], Ops::mul(coef, d2));
+  }
+
+  __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id) {
+    if (a.acc) {
+#pragma unroll
+      for (int cc = 0; cc < DIM; ++cc) ((R*)a.acc)[(size_t)id * DIM + cc] = acc[cc];
+      ((R*)a.drho)[id] = dr;
+    }
+    if (a.integrate) {
+      R* pos = (R*)a.pos;
+      R* vel = (R*)a.vel;
+      R* rho = (R*)a.rho;
+      if (id < K.fluid_end) {
+#pragma unroll
+        for (int cc = 0; cc < DIM; ++cc) {
+          const size_t o = (size_t)id * DIM + cc;
+          const R v = Ops::add(vel[o], Ops::mul(c.dt, Ops::add(acc[cc], c.g[cc])));
+          vel[o] = v;
+          pos[o] = Ops::add(pos[o], Ops::mul(c.dt, v));
+        }
+      }
+      rho[id] = Ops::add(rho[id], Ops::mul(c.dt, dr));
+    }
+  }
+};
+
+template <int DIM>
+struct DfPairs {
+  const float4 *Ah, *Al, *Bh, *Bl;
+  const float2* Rr;
+  const double4_32a* Xd;
+  SphDF w;
+  double four_h2;
+  double xid[3];
+  df xi[3], vi[3], rhoi, Pi;
+  df acc[3], dr;
+
+  __device__ __forceinline__ void begin(const SphArgs& a, const SphK& K, uint32_t k) {
+    Ah = (const float4*)a.s[0];
+    Al = (const float4*)a.s[1];
+    Bh = (const float4*)a.s[2];
+    Bl = (const float4*)a.s[3];
+    Rr = (const float2*)a.s[4];
+    Xd = (const double4_32a*)a.s[5];
+    w = K.w;
+    four_h2 = K.d.four_h2;
+    const float4 ah = Ah[k], al = Al[k], bh = Bh[k], bl = Bl[k];
+    const float2 rr = Rr[k];
+    xi[0] = df_make(ah.x, al.x); xi[1] = df_make(ah.y, al.y); xi[2] = df_make(ah.z, al.z);
+    vi[0] = df_make(bh.x, bl.x); vi[1] = df_make(bh.y, bl.y); vi[2] = df_make(bh.z, bl.z);
+    Pi = df_make(bh.w, bl.w);
+    rhoi = df_make(rr.x, rr.y);
+    const double4_32a xd = Xd[k];
+    xid[0] = xd.x; xid[1] = xd.y; xid[2] = xd.z;
+    acc[0] = acc[1] = acc[2] = df_make(0.f, 0.f);
+    dr = df_make(0.f, 0.f);
+  }
+
+  // The oracle's f64 neighbour test, used only when the double-word r^2 is within a relative
+  // band of 1e-9 of (2h)^2 (never, in practice).
+  __device__ __noinline__ bool exact_test(uint32_t t) const {
+    const double4_32a xj = Xd[t];
+    const double d0 = __dsub_rn(xid[0], xj.x), d1 = __dsub_rn(xid[1], xj.y);
+    double r2 = __dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1));
+    if (DIM == 3) {
+      const double d2 = __dsub_rn(xid[2], xj.z);
+      r2 = __dadd_rn(r2, __dmul_rn(d2, d2));
+    }
+    return r2 < four_h2 && r2 > 0.0;
+  }
+
+  __device__ __forceinline__ void pair(uint32_t t) {
+    const float4 ah = Ah[t], al = Al[t];
+    const df d0 = df_sub(xi[0], df_make(ah.x, al.x));
+    const df d1 = df_sub(xi[1], df_make(ah.y, al.y));
+    const df d2 = DIM == 3 ? df_sub(xi[2], df_make(ah.z, al.z)) : df_make(0.f, 0.f);
+    df r2 = df_add(df_mul(d0, d0), df_mul(d1, d1));
+    if (DIM == 3) r2 = df_add(r2, df_mul(d2, d2));
+    const df gap = df_sub(r2, df_make(w.four_h2[0], w.four_h2[1]));
+    if (fabsf(gap.hi) <= w.band) {
+      if (!exact_test(t)) return;
+    } else if (!(gap.hi < 0.f)) {
+      return;
+    }
+    if (!(r2.hi > 0.f)) return;
+    const df inv_r = df_rsqrt(r2);
+    const df r = df_mul(r2, inv_r);
+    const df q = df_mul(r, df_make(w.inv_h[0], w.inv_h[1]));
+    df F;
+    if (q.hi < 1.0f) {
+      F = df_mul(df_make(w.fa[0], w.fa[1]), df_add_f(df_mul_f(q, 2.25f), -3.0f));
+    } else {
+      const df tq = df_add_f(df_neg(q), 2.0f);
+      F = df_mul(df_mul(df_make(w.fb[0], w.fb[1]), df_mul(tq, tq)), inv_r);
+    }
+    const float4 bh = Bh[t], bl = Bl[t];
+    const df dv0 = df_sub(vi[0], df_make(bh.x, bl.x));
+    const df dv1 = df_sub(vi[1], df_make(bh.y, bl.y));
+    df wv = df_add(df_mul(dv0, d0), df_mul(dv1, d1));
+    if (DIM == 3) wv = df_add(wv, df_mul(df_sub(vi[2], df_make(bh.z, bl.z)), d2));
+    const df mj = df_make(ah.w, al.w);
+    dr = df_add(dr, df_mul(mj, df_mul(wv, F)));
+    df pij = df_make(0.f, 0.f);
+    if (wv.hi < 0.f) {
+      const float2 rj = Rr[t];
+      const df den = df_mul(df_add(r2, df_make(w.eps_h2[0], w.eps_h2[1])), df_add(rhoi, df_make(rj.x, rj.y)));
+      pij = df_div(df_mul(df_make(w.avk[0], w.avk[1]), wv), den);
+    }
+    const df coef = df_mul(mj, df_mul(df_add(df_add(Pi, df_make(bh.w, bl.w)), pij), F));
+    acc[0] = df_sub(acc[0], df_mul(coef, d0));
+    acc[1] = df_sub(acc[1], df_mul(coef, d1));
+    if (DIM == 3) acc[2] = df_sub(acc[2], df_mul(coef, d2));
+  }
+
+  __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id) {
+    double ad[3];
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) ad[cc] = df_to_double(acc[cc]);
+    const double drd = df_to_double(dr);
+    if (a.acc) {
+#pragma unroll
+      for (int cc = 0; cc < DIM; ++cc) ((double*)a.acc)[(size_t)id * DIM + cc] = ad[cc];
+      ((double*)a.drho)[id] = drd;
+    }
+    if (a.integrate) {
+      double* pos = (double*)a.pos;
+      double* vel = (double*)a.vel;
+      double* rho = (double*)a.rho;
+      const SphC<double>& c = K.d;
+      if (id < K.fluid_end) {
+#pragma unroll
+        for (int cc = 0; cc < DIM; ++cc) {
+          const size_t o = (size_t)id * DIM + cc;
+          const double v = __dadd_rn(vel[o], __dmul_rn(c.dt, __dadd_rn(ad[cc], c.g[cc])));
+          vel[o] = v;
+          pos[o] = __dadd_rn(pos[o], __dmul_rn(c.dt, v));
+        }
+      }
+      rho[id] = __dadd_rn(rho[id], __dmul_rn(c.dt, drd));
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------------------
+// The pass.  PF: the FP32 position array tested in phase 1 (float4 x,y,z per slot).
+// EXACT_PF: phase 1 is already the exact test (f32 systems); otherwise it is the
+// conservative bound and phase 2 repeats the exact test.
+// ---------------------------------------------------------------------------------------
+template <class Pairs, int DIM, bool EXACT_PF>
+__global__ void __launch_bounds__(kSphThreads) sph_pass_kernel(SphArgs a, int pf_index) {
+  __shared__ uint32_t hits[kHitCap][kSphThreads];
+  const int tid = threadIdx.x;
+  const float4* __restrict__ PF = (const float4*)a.s[pf_index];
+  const uint32_t* __restrict__ start = a.cell_start;
+  const int R = a.reach;
+  const int RZ = DIM == 3 ? R : 0;
+  const int side = 2 * R + 1;
+  const int nrows = side * (2 * RZ + 1);
+  const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
+
+  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint32_t k0 = tile * kSphThreads + tid;
+    const bool live = k0 < a.n;
+    const uint32_t k = live ? k0 : a.n - 1;
+    const uint32_t id = a.sorted_id[k];
+    const SphK& K = a.sys[sys_of_slot(a, id)];
+    const GridK& g = K.g;
+    const uint32_t c = a.sorted_cell[k] - g.cell_base;
+    const int cx = (int)(c % (uint32_t)g.nx);
+    const int cy = (int)((c / (uint32_t)g.nx) % (uint32_t)g.ny);
+    const int cz = (int)(c / ((uint32_t)g.nx * (uint32_t)g.ny));
+    const int x0 = max(cx - R, 0), x1 = min(cx + R, g.nx - 1);
+
+    Pairs P;
+    P.begin(a, K, k);
+    const float4 pi = PF[k];
+    float thr;
+    if (EXACT_PF) {
+      thr = K.f.four_h2;
+    } else {
+      // |x_j - x_i| < 2h in f64  =>  the FP32 r^2 below is < thr (rounding of positions to
+      // float and of the FP32 arithmetic bounded with a generous factor).
+      const float M = fmaxf(fmaxf(fabsf(pi.x), fabsf(pi.y)), fabsf(pi.z)) + K.two_h_f;
+      const float delta = 2.384185791015625e-07f * (2.f * M + K.two_h_f);  // 4u (2M + 2h)
+      const float rr = K.two_h_f + 2.f * delta;
+      thr = rr * rr * 1.0000153f;
+    }
+
+    int nh = 0;
+    int row = 0;
+    uint32_t t = 0, e = 0;
+    while (true) {
+      // advance this lane to its next candidate (rows z, y ascending)
+      while (t >= e && row < nrows) {
+        const int dz = row / side - RZ, dy = row % side - R;
+        ++row;
+        const int z = cz + dz, y = cy + dy;
+        if (!live || z < 0 || z >= g.nz || y < 0 || y >= g.ny) continue;
+        const uint32_t rb = g.cell_base + ((uint32_t)z * g.ny + (uint32_t)y) * g.nx;
+        t = start[rb + x0];
+        e = start[rb + x1 + 1];
+      }
+      const bool has = t < e;
+      if (has) {
+        const float4 pj = PF[t];
+        bool hit;
+        if (EXACT_PF) {
+          const float d0 = __fsub_rn(pi.x, pj.x), d1 = __fsub_rn(pi.y, pj.y);
+          float r2 = __fadd_rn(__fmul_rn(d0, d0), __fmul_rn(d1, d1));
+          if (DIM == 3) {
+            const float d2 = __fsub_rn(pi.z, pj.z);
+            r2 = __fadd_rn(r2, __fmul_rn(d2, d2));
+          }
+          hit = r2 < thr && r2 > 0.f;
+        } else {
+          const float d0 = pi.x - pj.x, d1 = pi.y - pj.y;
+          float r2 = fmaf(d1, d1, d0 * d0);
+          if (DIM == 3) {
+            const float d2 = pi.z - pj.z;
+            r2 = fmaf(d2, d2, r2);
+          }
+          hit = r2 < thr;
+        }
+        if (hit) hits[nh++][tid] = t;
+        ++t;
+      }
+      const bool done = !__any_sync(kFull, has);
+      if (done || __any_sync(kFull, nh == kHitCap)) {
+        for (int h = 0; __any_sync(kFull, h < nh); ++h)
+          if (h < nh) P.pair(hits[h][tid]);
+        nh = 0;
+        if (done) break;
+      }
+    }
+    if (live) P.finish(a, K, id);
+  }
+}
+
+template <class Pairs, int DIM, bool EXACT_PF>
+int launch_pass(cudaStream_t st, const SphArgs& a, int pf_index, int grid) {
+  if (a.n == 0) return PG_OK;
+  const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
+  if (grid <= 0 || (uint32_t)grid > ntiles) grid = (int)ntiles;
+  sph_pass_kernel<Pairs, DIM, EXACT_PF><<<grid, kSphThreads, 0, st>>>(a, pf_index);
+  return PG_OK;
+}
+
+}  // namespace
+
+void sph_sorted_layout(int arith, size_t sz[6]) {
+  for (int i = 0; i < 6; ++i) sz[i] = 0;
+  switch (arith) {
+    case ARITH_F64_EXACT:  // double4_32a A, double4_32a B, double P, float4 prefilter positions
+      sz[0] = 32; sz[1] = 32; sz[2] = 8; sz[3] = 16;
+      break;
+    case ARITH_F64_DF:  // float4 A.hi, A.lo, B.hi, B.lo, float2 rho, double4_32a exact positions
+      sz[0] = 16; sz[1] = 16; sz[2] = 16; sz[3] = 16; sz[4] = 8; sz[5] = 32;
+      break;
+    default:  // float4 A, float4 B, float P
+      sz[0] = 16; sz[1] = 16; sz[2] = 4;
+      break;
+  }
+}
+
+int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith) {
+  if (a.n == 0) return PG_OK;
+  const unsigned blocks = (a.n + 255) / 256;
+  const int dim = a.dim;
+  switch (arith) {
+    case ARITH_F64_EXACT:
+      if (dim == 2) sph_gather_real<OpsD, 2><<<blocks, 256, 0, st>>>(a);
+      else sph_gather_real<OpsD, 3><<<blocks, 256, 0, st>>>(a);
+      break;
+    case ARITH_F64_DF:
+      if (dim == 2) sph_gather_df<2><<<blocks, 256, 0, st>>>(a);
+      else sph_gather_df<3><<<blocks, 256, 0, st>>>(a);
+      break;
+    case ARITH_F32_EXACT:
+      if (dim == 2) sph_gather_real<OpsF, 2><<<blocks, 256, 0, st>>>(a);
+      else sph_gather_real<OpsF, 3><<<blocks, 256, 0, st>>>(a);
+      break;
+    case ARITH_F32_FAST:
+      if (dim == 2) sph_gather_real<OpsFF, 2><<<blocks, 256, 0, st>>>(a);
+      else sph_gather_real<OpsFF, 3><<<blocks, 256, 0, st>>>(a);
+      break;
+    default:
+      set_error("unknown arithmetic mode %d", arith);
+      return PG_EINVAL;
+  }
+  PG_CUDA_TRY(cudaGetLastError());
+  return PG_OK;
+}
+
+int launch_sph_pass(cudaStream_t st, const SphArgs& a, int arith, int grid) {
+  const int dim = a.dim;
+  int s = PG_OK;
+  switch (arith) {
+    case ARITH_F64_EXACT:
+      s = dim == 2 ? launch_pass<RealPairs<OpsD, 2, true>, 2, false>(st, a, 3, grid)
+                   : launch_pass<RealPairs<OpsD, 3, true>, 3, false>(st, a, 3, grid);
+      break;
+    case ARITH_F64_DF:
+      s = dim == 2 ? launch_pass<DfPairs<2>, 2, false>(st, a, 0, grid)
+                   : launch_pass<DfPairs<3>, 3, false>(st, a, 0, grid);
+      break;
+    case ARITH_F32_EXACT:
+      s = dim == 2 ? launch_pass<RealPairs<OpsF, 2, false>, 2, true>(st, a, 0, grid)
+                   : launch_pass<RealPairs<OpsF, 3, false>, 3, true>(st, a, 0, grid);
+      break;
+    case ARITH_F32_FAST:
+      s = dim == 2 ? launch_pass<RealPairs<OpsFF, 2, false>, 2, true>(st, a, 0, grid)
+                   : launch_pass<RealPairs<OpsFF, 3, false>, 3, true>(st, a, 0, grid);
+      break;
+    default:
+      set_error("unknown arithmetic mode %d", arith);
+      return PG_EINVAL;
+  }
+  if (s != PG_OK) return s;
+  PG_CUDA_TRY(cudaGetLastError());
+  return PG_OK;
+}
+
+int sph_pass_occupancy(int arith, int dim) {
+  int blocks = 0;
+  cudaError_t e = cudaSuccess;
+  switch (arith) {
+    case ARITH_F64_EXACT:
+      e = dim == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                         &blocks, sph_pass_kernel<RealPairs<OpsD, 2, true>, 2, false>, kSphThreads, 0)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                         &blocks, sph_pass_kernel<RealPairs<OpsD, 3, true>, 3, false>, kSphThreads, 0);
+      break;
+    case ARITH_F64_DF:
+      e = dim == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sph_pass_kernel<DfPairs<2>, 2, false>,
+                                                                   kSphThreads, 0)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sph_pass_kernel<DfPairs<3>, 3, false>,
+                                                                   kSphThreads, 0);
+      break;
+    case ARITH_F32_EXACT:
+      e = dim == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                         &blocks, sph_pass_kernel<RealPairs<OpsF, 2, false>, 2, true>, kSphThreads, 0)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                         &blocks, sph_pass_kernel<RealPairs<OpsF, 3, false>, 3, true>, kSphThreads, 0);
+      break;
+    default:
+      e = dim == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                         &blocks, sph_pass_kernel<RealPairs<OpsFF, 2, false>, 2, true>, kSphThreads, 0)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                         &blocks, sph_pass_kernel<RealPairs<OpsFF, 3, false>, 3, true>, kSphThreads, 0);
+      break;
+  }
+  if (e != cudaSuccess) return 0;
+  return blocks;
+}
+
+}  // namespace pg

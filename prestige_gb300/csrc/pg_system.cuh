@@ -1,0 +1,89 @@
+// The handle behind the opaque `pg_system*` of the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "pg_internal.cuh"
+#include "pg_kernels.cuh"
+
+struct pg_adjoint;  // checkpointed adjoint state (pg_adjoint.cu)
+
+struct pg_system {
+  // configuration
+  pg_config cfg;                   // system 0 (shared fields of a batch)
+  std::vector<pg_config> cfgs;     // one per system
+  std::vector<size_t> id_begin;    // n_systems + 1 entries
+  int model = PG_MODEL_SPH;
+  int dim = 3;
+  int f64 = 1;
+  int arith = 0;
+  size_t n = 0;
+  int nsys = 1;
+  cudaStream_t stream = nullptr;
+
+  // grids and per-system tables (device copies)
+  std::vector<pg::Grid> grids;
+  uint64_t ncells = 0;
+  pg::DevBuf gridk;      // GridK[nsys]
+  pg::DevBuf sys_of_id;  // u32[n] (batched handles only)
+  pg::DevBuf sphk;       // SphK[nsys]
+  pg::DevBuf demk;       // DemK
+
+  // canonical state, particle-id order
+  pg::DevBuf pos, vel, rho, mass;  // SPH: system precision; DEM: double
+  pg::DevBuf omega, radius;        // DEM
+  pg::DevBuf acc, drho;            // rates output (pg_compute_rates)
+  std::map<std::string, std::unique_ptr<pg::DevBuf>> user;  // user scalar fields (double)
+
+  // neighbour search and sorted copies
+  pg::NbrWork nw;
+  bool nbr_valid = false;
+  pg::DevBuf sorted[6];
+  pg::DevBuf spos;
+  pg::DevBuf tmp, tmp2, tmp3, tmp4;
+  int pass_grid = 0;
+
+  // DEM contact history, id order, double buffered
+  pg::DevBuf hpid[2], hxi[2];
+  int hcur = 0;
+  pg::DevBuf contacts;  // unsigned long long
+
+  // device error word
+  pg::DevBuf err;
+
+  // CUDA graph of one step (DEM: one per history parity)
+  bool graph_enabled = false;
+  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+
+  // step timing (pg_timing_enable): 4 events per step, consumed by pg_timing_read
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<cudaEvent_t> ev_pending;
+  pg_timing tacc;
+  long long launches = 0;  // kernels enqueued by this handle
+
+  // differentiable runs
+  pg_adjoint* adj = nullptr;
+  size_t adjoint_bytes() const;
+
+  ~pg_system();
+};
+
+namespace pg {
+size_t pg_elem_bytes(const pg_system* s);
+int ensure_sorted_buffers(pg_system* s);
+SphArgs sph_args(pg_system* s, int integrate, bool rates);
+int enqueue_neighbors(pg_system* s);
+int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev);
+long long neighbor_launches(const pg_system* s);
+int sync_and_check(pg_system* s);
+int choose_pass_grid(pg_system* s);
+void drop_graphs(pg_system* s);
+int capture_graphs(pg_system* s);
+void destroy_adjoint(pg_system* s);
+}  // namespace pg
