@@ -1,12 +1,436 @@
-// Placeholder: replaced by the checkpointed adjoint.
+// Reverse-mode differentiation of the SPH step (f64), with checkpointed recomputation.
+//
+// The reference has no differentiation; this is the adjoint of the forward step in pg_sph.cu
+// (continuity + Tait pressure + Monaghan viscosity as a gather into i over neighbours j, the
+// semantics of prestige/src/codegen/simple_cpu.rs:7-19, followed by the kick-drift update).
+//
+// Forward step t -> t+1 (fluid particles; wall particles keep x and v):
+//   v' = v + dt (a + g),  x' = x + dt v',  rho' = rho + dt drho
+// Given the adjoints (lx', lv', lr') of the state after the step, the adjoints before it are
+//   abar = dt (lv' + dt lx')   (fluid; 0 for walls),   dbar = dt lr'
+//   lx = lx' + dPhi/dx,  lv = (lv' + dt lx' | lv') + dPhi/dv,  lr = lr' + dPhi/drho
+// where Phi = sum_i (abar_i . a_i + dbar_i drho_i).  For one unordered pair (i, j) the two
+// ordered terms of Phi combine, because x_ji = -x_ij, v_ji = -v_ij and w, F, Pi_ij, P_i + P_j
+// are symmetric, into
+//   Lam = F (w D - S (x . E)),   D = dbar_i m_j + dbar_j m_i,   E = m_j abar_i - m_i abar_j,
+//   x = x_i - x_j,  v = v_i - v_j,  w = v . x,  S = P_i + P_j + Pi,  Pi = c1 w (w < 0, else 0),
+//   c1 = avk / ((r^2 + eps h^2)(rho_i + rho_j)),  F = (dW/dr)/r,  G = (dF/dr)/r
+// and its derivatives give particle i's share without any scatter:
+//   dLam/dx     = [G (w D - S xE) + 2 F xE Pi / (r^2 + eps h^2)] x + F (D - c1 xE) v - F S E
+//   dLam/dv     = F (D - c1 xE) x
+//   dLam/drho_i = -F xE (P'(rho_i) - Pi / (rho_i + rho_j))
+// with xE = x . E and P'(rho) = B ((gamma - 2)(rho/rho0)^gamma + 2) / rho^3.  Each thread
+// evaluates Lam for all its neighbours, so the transpose of the pair Jacobian is a second
+// gather over the same cell lists (no atomics, deterministic order).  The parameter
+// derivatives take only the ordered pair (i, j):
+//   dPhi/dalpha += -m_j F (abar_i . x) (-2 c0 h) w / ((r^2 + eps h^2)(rho_i + rho_j))  (w < 0)
+//   dPhi/dB     += -m_j F (abar_i . x) (P_i + P_j) / B
+// accumulated per particle and summed in a fixed order at the end.
+//
+// Checkpointing: pg_forward_checkpointed keeps the state every `every` steps.  pg_backward
+// walks the segments last to first; for each it restores the checkpoint, re-runs the forward
+// steps while keeping each step's state and its neighbour structure (sorted cells, sorted ids,
+// cell table: integer data, reused as is), then sweeps the adjoint back through the segment.
+// Memory: (nsteps / every) checkpoints plus one segment of `every` steps.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "pg_arith.cuh"
+#include "pg_internal.cuh"
+#include "pg_kernels.cuh"
+#include "pg_sph_pass.cuh"
 #include "pg_system.cuh"
-struct pg_adjoint {};
-size_t pg_system::adjoint_bytes() const { return 0; }
+
+struct pg_adjoint {
+  int nsteps = 0, every = 0, nseg = 0;
+  bool have_forward = false;
+  size_t state_doubles = 0;  // n * (2 dim + 1): pos, vel, rho
+  pg::DevBuf ckpt;           // nseg states
+  pg::DevBuf final_state;
+  pg::DevBuf seg_state;      // `every` states of the segment being swept
+  pg::DevBuf seg_cell, seg_id, seg_start;
+  pg::DevBuf lx, lv, lr, ga, gb;
+  pg::DevBuf X4, V4, Q4, A4, PF;  // slot-ordered packs of one adjoint step
+  int pass_grid = 0;
+  size_t bytes() const {
+    const pg::DevBuf* b[] = {&ckpt, &final_state, &seg_state, &seg_cell, &seg_id, &seg_start, &lx, &lv,
+                             &lr,    &ga,          &gb,         &X4,       &V4,     &Q4,        &A4, &PF};
+    size_t t = 0;
+    for (const pg::DevBuf* d : b) t += d->bytes;
+    return t;
+  }
+};
+
+size_t pg_system::adjoint_bytes() const { return adj ? adj->bytes() : 0; }
+
 namespace pg {
-void destroy_adjoint(pg_system* s) { delete s->adj; s->adj = nullptr; }
+
+void destroy_adjoint(pg_system* s) {
+  delete s->adj;
+  s->adj = nullptr;
 }
+
+namespace {
+
+using namespace sphpass;
+
+// Slot-ordered packs for one adjoint step:
+//   X4 {x, y, z, m}   V4 {vx, vy, vz, rho}   Q4 {P, P'(rho), P/B, dbar}   A4 {abar, 0}   PF float4 x
+template <int DIM>
+__global__ void adjoint_prep_kernel(SphArgs a) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.n) return;
+  const uint32_t id = a.sorted_id[k];
+  const SphK& K = a.sys[0];
+  const double* pos = (const double*)a.pos;
+  const double* vel = (const double*)a.vel;
+  const double* lx = (const double*)a.lam[0];
+  const double* lv = (const double*)a.lam[1];
+  const double* lr = (const double*)a.lam[2];
+  const double rho = ((const double*)a.rho)[id];
+  const double m = ((const double*)a.mass)[id];
+  const double dt = K.d.dt;
+  const bool fluid = id < K.fluid_end;
+  double x[3] = {0, 0, 0}, v[3] = {0, 0, 0}, ab[3] = {0, 0, 0};
+#pragma unroll
+  for (int c = 0; c < DIM; ++c) {
+    const size_t o = (size_t)id * DIM + c;
+    x[c] = pos[o];
+    v[c] = vel[o];
+    ab[c] = fluid ? dt * (lv[o] + dt * lx[o]) : 0.0;
+  }
+  const double rr = rho * K.d.inv_rho0;
+  double pw = rr;
+  for (int e = 1; e < K.gamma; ++e) pw *= rr;
+  const double inv_r2 = 1.0 / (rho * rho);
+  const double P = tait_pterm<OpsD>(K.d, K.gamma, rho);
+  const double Pd = K.d.B * ((double)(K.gamma - 2) * pw + 2.0) * inv_r2 / rho;
+  const double PB = (pw - 1.0) * inv_r2;
+  ((double4_32a*)a.s[0])[k] = make_double4_32a(x[0], x[1], x[2], m);
+  ((double4_32a*)a.s[1])[k] = make_double4_32a(v[0], v[1], v[2], rho);
+  ((double4_32a*)a.s[2])[k] = make_double4_32a(P, Pd, PB, dt * lr[id]);
+  ((double4_32a*)a.s[3])[k] = make_double4_32a(ab[0], ab[1], ab[2], 0.0);
+  ((float4*)a.s[4])[k] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
+}
+
+template <int DIM>
+struct AdjPairs {
+  const double4_32a *X, *V, *Q, *A;
+  double fa, fb, inv_h, four_h2, eps_h2, avk, avk_alpha;
+  double xi[3], vi[3], ai[3], rhoi, mi, Pi, Pdi, PBi, dbi;
+  double gx[3], gv[3], gr, gal, gB;
+
+  __device__ __forceinline__ void begin(const SphArgs& a, const SphK& K, uint32_t k) {
+    X = (const double4_32a*)a.s[0];
+    V = (const double4_32a*)a.s[1];
+    Q = (const double4_32a*)a.s[2];
+    A = (const double4_32a*)a.s[3];
+    fa = K.d.fa;
+    fb = K.d.fb;
+    inv_h = K.d.inv_h;
+    four_h2 = K.d.four_h2;
+    eps_h2 = K.d.eps_h2;
+    avk = K.d.avk;
+    avk_alpha = K.avk_alpha;
+    const double4_32a x = X[k], v = V[k], q = Q[k], ab = A[k];
+    xi[0] = x.x; xi[1] = x.y; xi[2] = x.z; mi = x.w;
+    vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; rhoi = v.w;
+    Pi = q.x; Pdi = q.y; PBi = q.z; dbi = q.w;
+    ai[0] = ab.x; ai[1] = ab.y; ai[2] = ab.z;
+    gx[0] = gx[1] = gx[2] = 0.0;
+    gv[0] = gv[1] = gv[2] = 0.0;
+    gr = gal = gB = 0.0;
+  }
+
+  __device__ __forceinline__ void pair(uint32_t t) {
+    const double4_32a xj = X[t];
+    double d[3] = {xi[0] - xj.x, xi[1] - xj.y, DIM == 3 ? xi[2] - xj.z : 0.0};
+    // the forward pass's neighbour test, same operation order
+    double r2 = __dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1]));
+    if (DIM == 3) r2 = __dadd_rn(r2, __dmul_rn(d[2], d[2]));
+    if (!(r2 < four_h2) || !(r2 > 0.0)) return;
+    const double4_32a vj = V[t], qj = Q[t], aj = A[t];
+    const double mj = xj.w, rhoj = vj.w;
+    const double r = sqrt(r2);
+    const double inv_r = 1.0 / r;
+    const double q = r * inv_h;
+    double F, G;
+    if (q < 1.0) {
+      F = fa * (2.25 * q - 3.0);
+      G = fa * 2.25 * inv_h * inv_r;
+    } else {
+      const double tq = 2.0 - q;
+      F = fb * tq * tq * inv_r;
+      G = -(fb * tq * inv_r) * (2.0 * inv_h + tq * inv_r) * inv_r;
+    }
+    const double dv[3] = {vi[0] - vj.x, vi[1] - vj.y, DIM == 3 ? vi[2] - vj.z : 0.0};
+    double w = dv[0] * d[0] + dv[1] * d[1];
+    if (DIM == 3) w += dv[2] * d[2];
+    const double rb = rhoi + rhoj;
+    const double e = r2 + eps_h2;
+    double c1 = 0.0, c1a = 0.0;
+    if (w < 0.0) {
+      const double base = 1.0 / (e * rb);
+      c1 = avk * base;
+      c1a = avk_alpha * base;
+    }
+    const double PI = c1 * w;
+    const double S = Pi + qj.x + PI;
+    const double D = dbi * mj + qj.w * mi;
+    double E[3], xE = 0.0, axd = 0.0;
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+      E[c] = mj * ai[c] - mi * (c == 0 ? aj.x : c == 1 ? aj.y : aj.z);
+      xE += d[c] * E[c];
+      axd += ai[c] * d[c];
+    }
+    const double a1 = G * (w * D - S * xE) + 2.0 * F * xE * PI / e;
+    const double b1 = F * (D - c1 * xE);
+    const double fs = F * S;
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+      gx[c] += a1 * d[c] + b1 * dv[c] - fs * E[c];
+      gv[c] += b1 * d[c];
+    }
+    gr -= F * xE * (Pdi - PI / rb);
+    const double own = mj * F * axd;
+    gal -= own * c1a * w;
+    gB -= own * (PBi + qj.z);
+  }
+
+  __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id) {
+    double* lx = (double*)a.lam[0];
+    double* lv = (double*)a.lam[1];
+    double* lr = (double*)a.lam[2];
+    const bool fluid = id < K.fluid_end;
+    const double dt = K.d.dt;
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+      const size_t o = (size_t)id * DIM + c;
+      const double lxo = lx[o];
+      lx[o] = lxo + gx[c];
+      lv[o] = (fluid ? lv[o] + dt * lxo : lv[o]) + gv[c];
+    }
+    lr[id] += gr;
+    ((double*)a.lam[3])[id] += gal;
+    ((double*)a.lam[4])[id] += gB;
+  }
+};
+
+}  // namespace
+
+int launch_adjoint_prep(cudaStream_t st, const SphArgs& a) {
+  if (a.n == 0) return PG_OK;
+  const unsigned b = (a.n + 255) / 256;
+  if (a.dim == 2) adjoint_prep_kernel<2><<<b, 256, 0, st>>>(a);
+  else adjoint_prep_kernel<3><<<b, 256, 0, st>>>(a);
+  PG_CUDA_TRY(cudaGetLastError());
+  return PG_OK;
+}
+
+int launch_adjoint_pass(cudaStream_t st, const SphArgs& a, int grid) {
+  if (a.n == 0) return PG_OK;
+  const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
+  if (grid <= 0 || (uint32_t)grid > ntiles) grid = (int)ntiles;
+  if (a.dim == 2) sph_pass_kernel<AdjPairs<2>, 2, false><<<grid, kSphThreads, 0, st>>>(a, 4);
+  else sph_pass_kernel<AdjPairs<3>, 3, false><<<grid, kSphThreads, 0, st>>>(a, 4);
+  PG_CUDA_TRY(cudaGetLastError());
+  return PG_OK;
+}
+
+int adjoint_pass_occupancy(int dim) {
+  int blocks = 0;
+  cudaError_t e =
+      dim == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sph_pass_kernel<AdjPairs<2>, 2, false>,
+                                                               kSphThreads, 0)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sph_pass_kernel<AdjPairs<3>, 3, false>,
+                                                               kSphThreads, 0);
+  return e == cudaSuccess ? blocks : 0;
+}
+
+namespace {
+
+int copy_state_out(pg_system* s, double* dst) {
+  const size_t nd = s->n * (size_t)s->dim;
+  PG_CUDA_TRY(cudaMemcpyAsync(dst, s->pos.p, 8 * nd, cudaMemcpyDeviceToDevice, s->stream));
+  PG_CUDA_TRY(cudaMemcpyAsync(dst + nd, s->vel.p, 8 * nd, cudaMemcpyDeviceToDevice, s->stream));
+  PG_CUDA_TRY(cudaMemcpyAsync(dst + 2 * nd, s->rho.p, 8 * s->n, cudaMemcpyDeviceToDevice, s->stream));
+  return PG_OK;
+}
+
+int copy_state_in(pg_system* s, const double* src) {
+  const size_t nd = s->n * (size_t)s->dim;
+  PG_CUDA_TRY(cudaMemcpyAsync(s->pos.p, src, 8 * nd, cudaMemcpyDeviceToDevice, s->stream));
+  PG_CUDA_TRY(cudaMemcpyAsync(s->vel.p, src + nd, 8 * nd, cudaMemcpyDeviceToDevice, s->stream));
+  PG_CUDA_TRY(cudaMemcpyAsync(s->rho.p, src + 2 * nd, 8 * s->n, cudaMemcpyDeviceToDevice, s->stream));
+  return PG_OK;
+}
+
+int check_differentiable(pg_system* s) {
+  if (s->model != PG_MODEL_SPH || s->nsys != 1 || !s->f64) {
+    set_error("differentiation needs a single double-precision SPH system");
+    return PG_EINVAL;
+  }
+  return PG_OK;
+}
+
+}  // namespace
+
+}  // namespace pg
+
 extern "C" {
-int pg_forward_checkpointed(pg_system*, int, int) { pg::set_error("not built"); return PG_ESTATE; }
-int pg_backward(pg_system*, const double*, double*, double*, double*) { pg::set_error("not built"); return PG_ESTATE; }
-int pg_autotune(pg_system*, int, int*, double*, int*, double*) { pg::set_error("not built"); return PG_ESTATE; }
+
+int pg_forward_checkpointed(pg_system* s, int nsteps, int every) {
+  pg::clear_error();
+  if (!s) {
+    pg::set_error("null handle");
+    return PG_EINVAL;
+  }
+  PG_TRY(pg::check_differentiable(s));
+  if (nsteps < 0 || every < 1) {
+    pg::set_error("need nsteps >= 0 and every >= 1");
+    return PG_EINVAL;
+  }
+  if (!s->adj) s->adj = new pg_adjoint();
+  pg_adjoint* A = s->adj;
+  A->have_forward = false;
+  A->nsteps = nsteps;
+  A->every = every;
+  A->nseg = (nsteps + every - 1) / every;
+  A->state_doubles = s->n * (size_t)(2 * s->dim + 1);
+  const size_t sb = 8 * (A->state_doubles ? A->state_doubles : 1);
+  PG_TRY(A->ckpt.ensure(sb * (A->nseg ? A->nseg : 1)));
+  PG_TRY(A->final_state.ensure(sb));
+  for (int seg = 0; seg < A->nseg; ++seg) {
+    PG_TRY(pg::copy_state_out(s, A->ckpt.as<double>() + (size_t)seg * A->state_doubles));
+    const int steps = std::min(every, nsteps - seg * every);
+    for (int t = 0; t < steps; ++t) PG_TRY(pg::enqueue_sph_step(s, false, 1, nullptr));
+  }
+  PG_TRY(pg::copy_state_out(s, A->final_state.as<double>()));
+  PG_TRY(pg::sync_and_check(s));
+  s->nbr_valid = false;
+  A->have_forward = true;
+  return PG_OK;
 }
+
+int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL_dB, double* dL_dv0) {
+  pg::clear_error();
+  if (!s) {
+    pg::set_error("null handle");
+    return PG_EINVAL;
+  }
+  PG_TRY(pg::check_differentiable(s));
+  pg_adjoint* A = s->adj;
+  if (!A || !A->have_forward) {
+    pg::set_error("call pg_forward_checkpointed first");
+    return PG_ESTATE;
+  }
+  if (!dL_dx && s->n) {
+    pg::set_error("null dL/dx");
+    return PG_EINVAL;
+  }
+  const size_t n = s->n, nn = n ? n : 1, nd = n * (size_t)s->dim;
+  const size_t ncp1 = s->ncells + 1;
+  const int every = A->every;
+  PG_TRY(A->seg_state.ensure(8 * A->state_doubles * every + 8));
+  PG_TRY(A->seg_cell.ensure(4 * nn * every));
+  PG_TRY(A->seg_id.ensure(4 * nn * every));
+  PG_TRY(A->seg_start.ensure(4 * ncp1 * every));
+  PG_TRY(A->lx.ensure(8 * nn * s->dim));
+  PG_TRY(A->lv.ensure(8 * nn * s->dim));
+  PG_TRY(A->lr.ensure(8 * nn));
+  PG_TRY(A->ga.ensure(8 * nn));
+  PG_TRY(A->gb.ensure(8 * nn));
+  PG_TRY(A->X4.ensure(32 * nn));
+  PG_TRY(A->V4.ensure(32 * nn));
+  PG_TRY(A->Q4.ensure(32 * nn));
+  PG_TRY(A->A4.ensure(32 * nn));
+  PG_TRY(A->PF.ensure(16 * nn));
+  if (A->pass_grid == 0) {
+    int dev = 0, sms = 0;
+    PG_CUDA_TRY(cudaGetDevice(&dev));
+    PG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    A->pass_grid = pg::adjoint_pass_occupancy(s->dim) * sms;
+  }
+  if (nd) PG_CUDA_TRY(cudaMemcpyAsync(A->lx.p, dL_dx, 8 * nd, cudaMemcpyHostToDevice, s->stream));
+  PG_CUDA_TRY(cudaMemsetAsync(A->lv.p, 0, 8 * nn * s->dim, s->stream));
+  PG_CUDA_TRY(cudaMemsetAsync(A->lr.p, 0, 8 * nn, s->stream));
+  PG_CUDA_TRY(cudaMemsetAsync(A->ga.p, 0, 8 * nn, s->stream));
+  PG_CUDA_TRY(cudaMemsetAsync(A->gb.p, 0, 8 * nn, s->stream));
+
+  pg::SphArgs a = pg::sph_args(s, 0, false);
+  a.s[0] = A->X4.p;
+  a.s[1] = A->V4.p;
+  a.s[2] = A->Q4.p;
+  a.s[3] = A->A4.p;
+  a.s[4] = A->PF.p;
+  a.s[5] = nullptr;
+  a.lam[0] = A->lx.p;
+  a.lam[1] = A->lv.p;
+  a.lam[2] = A->lr.p;
+  a.lam[3] = A->ga.p;
+  a.lam[4] = A->gb.p;
+
+  for (int seg = A->nseg - 1; seg >= 0; --seg) {
+    const int steps = std::min(every, A->nsteps - seg * every);
+    // recompute the segment, keeping each step's state and neighbour structure
+    PG_TRY(pg::copy_state_in(s, A->ckpt.as<double>() + (size_t)seg * A->state_doubles));
+    for (int t = 0; t < steps; ++t) {
+      PG_TRY(pg::copy_state_out(s, A->seg_state.as<double>() + (size_t)t * A->state_doubles));
+      if (t + 1 < steps) {
+        PG_TRY(pg::enqueue_sph_step(s, false, 1, nullptr));
+      } else {
+        PG_TRY(pg::enqueue_neighbors(s));
+      }
+      if (n) {
+        PG_CUDA_TRY(cudaMemcpyAsync(A->seg_cell.as<uint32_t>() + (size_t)t * n, s->nw.sorted_cell, 4 * n,
+                                    cudaMemcpyDeviceToDevice, s->stream));
+        PG_CUDA_TRY(cudaMemcpyAsync(A->seg_id.as<uint32_t>() + (size_t)t * n, s->nw.sorted_id, 4 * n,
+                                    cudaMemcpyDeviceToDevice, s->stream));
+      }
+      PG_CUDA_TRY(cudaMemcpyAsync(A->seg_start.as<uint32_t>() + (size_t)t * ncp1, s->nw.cell_start.p, 4 * ncp1,
+                                  cudaMemcpyDeviceToDevice, s->stream));
+    }
+    // sweep the adjoint back through the segment
+    for (int t = steps - 1; t >= 0; --t) {
+      const double* st = A->seg_state.as<double>() + (size_t)t * A->state_doubles;
+      a.pos = (void*)st;
+      a.vel = (void*)(st + nd);
+      a.rho = (void*)(st + 2 * nd);
+      a.sorted_cell = A->seg_cell.as<uint32_t>() + (size_t)t * n;
+      a.sorted_id = A->seg_id.as<uint32_t>() + (size_t)t * n;
+      a.cell_start = A->seg_start.as<uint32_t>() + (size_t)t * ncp1;
+      PG_TRY(pg::launch_adjoint_prep(s->stream, a));
+      PG_TRY(pg::launch_adjoint_pass(s->stream, a, A->pass_grid));
+    }
+  }
+  PG_TRY(pg::copy_state_in(s, A->final_state.as<double>()));
+  std::vector<double> ga(n), gb(n);
+  if (n) {
+    PG_CUDA_TRY(cudaMemcpyAsync(ga.data(), A->ga.p, 8 * n, cudaMemcpyDeviceToHost, s->stream));
+    PG_CUDA_TRY(cudaMemcpyAsync(gb.data(), A->gb.p, 8 * n, cudaMemcpyDeviceToHost, s->stream));
+    if (dL_dv0) PG_CUDA_TRY(cudaMemcpyAsync(dL_dv0, A->lv.p, 8 * nd, cudaMemcpyDeviceToHost, s->stream));
+  }
+  PG_TRY(pg::sync_and_check(s));
+  s->nbr_valid = false;
+  // fixed-order pairwise sums of the per-particle partials
+  auto tree_sum = [](std::vector<double>& v) {
+    size_t m = v.size();
+    if (m == 0) return 0.0;
+    while (m > 1) {
+      const size_t h = (m + 1) / 2;
+      for (size_t i = 0; i + h < m; ++i) v[i] += v[i + h];
+      m = h;
+    }
+    return v[0];
+  };
+  if (dL_dalpha) *dL_dalpha = tree_sum(ga);
+  if (dL_dB) *dL_dB = tree_sum(gb);
+  return PG_OK;
+}
+
+}  // extern "C"

@@ -53,6 +53,7 @@ SphK make_sphk(const pg_config& c, const Grid& g, uint32_t cell_base, uint32_t i
   k.d.inv_h = 1.0 / h;
   k.d.four_h2 = (2.0 * h) * (2.0 * h);
   k.d.avk = (-2.0 * c.c0 * h) * c.alpha;
+  k.avk_alpha = -2.0 * c.c0 * h;
   k.d.eps_h2 = c.eps_av * h * h;
   k.d.B = B;
   k.d.inv_rho0 = 1.0 / c.rho0;

@@ -36,6 +36,7 @@ struct SphK {
   SphC<float> f;
   SphDF w;
   float two_h_f;
+  double avk_alpha;                      // d avk / d alpha = -2 c0 h (adjoint)
   uint32_t id_begin, id_end, fluid_end;  // global ids; ids >= fluid_end are fixed wall particles
   int gamma;
 };
@@ -55,12 +56,20 @@ struct SphArgs {
   void* mass;
   void* acc;                 // optional rates output, id order
   void* drho;
+  void* lam[5];              // adjoint (pg_adjoint.cu): lambda_x, lambda_v, lambda_rho, dL/dalpha and
+                             // dL/dB partial sums, all id order
   int integrate;
 };
 
 int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith);
 int launch_sph_pass(cudaStream_t st, const SphArgs& a, int arith, int grid);
 int sph_pass_occupancy(int arith, int dim);
+
+// Adjoint of one SPH step (pg_adjoint.cu).  s[0..4] hold the slot-ordered packs written by
+// launch_adjoint_prep; pos/vel/rho/mass are the state before the step (id order).
+int launch_adjoint_prep(cudaStream_t st, const SphArgs& a);
+int launch_adjoint_pass(cudaStream_t st, const SphArgs& a, int grid);
+int adjoint_pass_occupancy(int dim);
 // Bytes per particle of the sorted packed arrays s[0..5] for an arithmetic mode.
 void sph_sorted_layout(int arith, size_t sizes[6]);
 

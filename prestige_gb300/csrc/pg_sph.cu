@@ -26,37 +26,13 @@
 #include "pg_arith.cuh"
 #include "pg_internal.cuh"
 #include "pg_kernels.cuh"
+#include "pg_sph_pass.cuh"
 
 namespace pg {
 
 namespace {
 
-constexpr int kHitCap = 32;
-constexpr unsigned kFull = 0xffffffffu;
-
-template <class R> struct V4;
-template <> struct V4<double> { typedef double4_32a T; };
-template <> struct V4<float> { typedef float4 T; };
-
-template <class R> __device__ __forceinline__ const SphC<R>& consts(const SphK& K);
-template <> __device__ __forceinline__ const SphC<double>& consts<double>(const SphK& K) { return K.d; }
-template <> __device__ __forceinline__ const SphC<float>& consts<float>(const SphK& K) { return K.f; }
-
-// p / rho^2 with p = B((rho/rho0)^gamma - 1), operation order of the oracle's tait_pterm.
-template <class Ops>
-__device__ __forceinline__ typename Ops::R tait_pterm(const SphC<typename Ops::R>& c, int gamma,
-                                                      typename Ops::R rho) {
-  typedef typename Ops::R R;
-  const R rr = Ops::mul(rho, c.inv_rho0);
-  R pw = rr;
-  for (int e = 1; e < gamma; ++e) pw = Ops::mul(pw, rr);
-  const R p = Ops::mul(c.B, Ops::sub(pw, R(1)));
-  return Ops::div(p, Ops::mul(rho, rho));
-}
-
-__device__ __forceinline__ uint32_t sys_of_slot(const SphArgs& a, uint32_t id) {
-  return a.sys_of_id ? a.sys_of_id[id] : 0u;
-}
+using namespace sphpass;
 
 // ---------------------------------------------------------------------------------------
 // Sorted gather: slot k <- particle sorted_id[k]; precomputes P = p / rho^2.
@@ -330,101 +306,6 @@ struct DfPairs {
     }
   }
 };
-
-// ---------------------------------------------------------------------------------------
-// The pass.  PF: the FP32 position array tested in phase 1 (float4 x,y,z per slot).
-// EXACT_PF: phase 1 is already the exact test (f32 systems); otherwise it is the
-// conservative bound and phase 2 repeats the exact test.
-// ---------------------------------------------------------------------------------------
-template <class Pairs, int DIM, bool EXACT_PF>
-__global__ void __launch_bounds__(kSphThreads) sph_pass_kernel(SphArgs a, int pf_index) {
-  __shared__ uint32_t hits[kHitCap][kSphThreads];
-  const int tid = threadIdx.x;
-  const float4* __restrict__ PF = (const float4*)a.s[pf_index];
-  const uint32_t* __restrict__ start = a.cell_start;
-  const int R = a.reach;
-  const int RZ = DIM == 3 ? R : 0;
-  const int side = 2 * R + 1;
-  const int nrows = side * (2 * RZ + 1);
-  const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
-
-  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const uint32_t k0 = tile * kSphThreads + tid;
-    const bool live = k0 < a.n;
-    const uint32_t k = live ? k0 : a.n - 1;
-    const uint32_t id = a.sorted_id[k];
-    const SphK& K = a.sys[sys_of_slot(a, id)];
-    const GridK& g = K.g;
-    const uint32_t c = a.sorted_cell[k] - g.cell_base;
-    const int cx = (int)(c % (uint32_t)g.nx);
-    const int cy = (int)((c / (uint32_t)g.nx) % (uint32_t)g.ny);
-    const int cz = (int)(c / ((uint32_t)g.nx * (uint32_t)g.ny));
-    const int x0 = max(cx - R, 0), x1 = min(cx + R, g.nx - 1);
-
-    Pairs P;
-    P.begin(a, K, k);
-    const float4 pi = PF[k];
-    float thr;
-    if (EXACT_PF) {
-      thr = K.f.four_h2;
-    } else {
-      // |x_j - x_i| < 2h in f64  =>  the FP32 r^2 below is < thr (rounding of positions to
-      // float and of the FP32 arithmetic bounded with a generous factor).
-      const float M = fmaxf(fmaxf(fabsf(pi.x), fabsf(pi.y)), fabsf(pi.z)) + K.two_h_f;
-      const float delta = 2.384185791015625e-07f * (2.f * M + K.two_h_f);  // 4u (2M + 2h)
-      const float rr = K.two_h_f + 2.f * delta;
-      thr = rr * rr * 1.0000153f;
-    }
-
-    int nh = 0;
-    int row = 0;
-    uint32_t t = 0, e = 0;
-    while (true) {
-      // advance this lane to its next candidate (rows z, y ascending)
-      while (t >= e && row < nrows) {
-        const int dz = row / side - RZ, dy = row % side - R;
-        ++row;
-        const int z = cz + dz, y = cy + dy;
-        if (!live || z < 0 || z >= g.nz || y < 0 || y >= g.ny) continue;
-        const uint32_t rb = g.cell_base + ((uint32_t)z * g.ny + (uint32_t)y) * g.nx;
-        t = start[rb + x0];
-        e = start[rb + x1 + 1];
-      }
-      const bool has = t < e;
-      if (has) {
-        const float4 pj = PF[t];
-        bool hit;
-        if (EXACT_PF) {
-          const float d0 = __fsub_rn(pi.x, pj.x), d1 = __fsub_rn(pi.y, pj.y);
-          float r2 = __fadd_rn(__fmul_rn(d0, d0), __fmul_rn(d1, d1));
-          if (DIM == 3) {
-            const float d2 = __fsub_rn(pi.z, pj.z);
-            r2 = __fadd_rn(r2, __fmul_rn(d2, d2));
-          }
-          hit = r2 < thr && r2 > 0.f;
-        } else {
-          const float d0 = pi.x - pj.x, d1 = pi.y - pj.y;
-          float r2 = fmaf(d1, d1, d0 * d0);
-          if (DIM == 3) {
-            const float d2 = pi.z - pj.z;
-            r2 = fmaf(d2, d2, r2);
-          }
-          hit = r2 < thr;
-        }
-        if (hit) hits[nh++][tid] = t;
-        ++t;
-      }
-      const bool done = !__any_sync(kFull, has);
-      if (done || __any_sync(kFull, nh == kHitCap)) {
-        for (int h = 0; __any_sync(kFull, h < nh); ++h)
-          if (h < nh) P.pair(hits[h][tid]);
-        nh = 0;
-        if (done) break;
-      }
-    }
-    if (live) P.finish(a, K, id);
-  }
-}
 
 template <class Pairs, int DIM, bool EXACT_PF>
 int launch_pass(cudaStream_t st, const SphArgs& a, int pf_index, int grid) {
