@@ -3,8 +3,8 @@
 Workload (default): 4,096,000 particles (160^3 jittered cubic lattice, dx = 0.01, h = 1.3 dx,
 v ~ N(0, 0.1), rho = 1000 (1 + U(-0.01, 0.01))), double precision, f64 fast arithmetic
 (double-word pair terms within the 1e-10 f64 tolerance; `--mode native` for IEEE double).
-A step = cell hash + stable radix sort + cell table + sorted gather + fused pair pass with
-the integrator.  The state (4M x 64 B = 256 MB) is larger than the 129 MB L2, so no flush is
+A step = cell hash + stable radix sort + cell table + sorted gather + continuity pass (density
+update) + momentum pass (velocity and position update).  The state (4M x 64 B = 256 MB) is larger than the 129 MB L2, so no flush is
 needed between steps.
 
 Output: one JSON line (rank 0).  `value` = particle-steps/s over the timed steps with the state
@@ -168,7 +168,7 @@ def workload(args, n=None):
 def config_json(args, n):
     return {"workload": "sph_lattice_3d", "particles": n, "lattice": "jittered cubic, dx=0.01, jitter +-0.2dx",
             "h_over_dx": 1.3, "precision": args.precision, "arith": args.mode,
-            "step": "hash+radix sort+cell table+sorted gather+fused pair pass+integrator",
+            "step": "hash+radix sort+cell table+sorted gather+continuity pass+momentum pass (symplectic Euler)",
             "l2": "state larger than L2 (no flush)", "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
 
 

@@ -144,7 +144,9 @@ int pg_gather_sum(pg_system* sys, const char* dst, const char* src);
  * (prestige/src/equations/fuse.rs:14-40, prestige/src/codegen/simple_cpu.rs:3-22). */
 int pg_compute_rates(pg_system* sys);
 
-/* Advance nsteps full steps (neighbour search + pair pass + integrator) and wait for them.
+/* Advance nsteps full steps and wait for them.  SPH step: neighbour search, continuity pass
+ * (rho' = rho + dt drho), momentum pass with rho' (v' = v + dt (a + g), x' = x + dt v';
+ * wall particles keep x and v).  DEM step: neighbour search, contact pass + integrator.
  * pg_step_async only enqueues them on the handle's stream; pg_sync waits and reports
  * device-side errors (PG_EOVERFLOW for DEM contact slots). */
 int pg_step(pg_system* sys, int nsteps);
@@ -182,9 +184,10 @@ typedef struct pg_timing {
   double region_ms;    /* first timed step start -> last timed step end */
   double neighbor_ms;  /* hash + sort + cell table, summed over steps */
   double gather_ms;    /* sorted copies, summed */
-  double pass_ms;      /* pair pass + integrator, summed */
+  double pass_ms;      /* pair passes + integrator, summed */
   long long steps;
   long long launches;  /* kernels launched by the timed steps */
+  double cont_ms;      /* SPH continuity pass alone (part of pass_ms), summed */
 } pg_timing;
 int pg_timing_enable(pg_system* sys, int enable);
 int pg_timing_read(pg_system* sys, pg_timing* out);

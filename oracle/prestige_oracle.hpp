@@ -257,7 +257,7 @@ void gather_sum(const CellList& cl, size_t n, const P* const* pos, P support, co
 // Artificial viscosity (Monaghan 1992) with c_ij = c0, rho_ij = (rho_i + rho_j)/2:
 //   Pi_ij = -alpha c0 mu_ij / rho_ij,  mu_ij = h v_ij.x_ij / (r^2 + eps h^2)   if v_ij.x_ij < 0
 //         = avk * w / ((r^2 + eps h^2) (rho_i + rho_j)),  avk = -2 alpha c0 h.
-// Kick-drift: v' = v + dt a; x' = x + dt v'; rho' = rho + dt drho.
+// Time step (sph_step): rho' = rho + dt drho(x, v); v' = v + dt (a(x, v, rho') + g); x' = x + dt v'.
 // Particles with id >= n_fluid are fixed dummy-wall particles: x, v fixed, rho evolves.
 // ----------------------------------------------------------------------------------------
 struct SphSpec {
@@ -325,15 +325,17 @@ struct SphState {
   }
 };
 
-// One SPH rate evaluation for particle i.  Neighbour order is that of for_each_candidate.
-template <class T, int DIM>
+// Pair loop for particle i in the order of for_each_candidate.  CONT accumulates the
+// continuity rate, MOM the momentum rate; both share the neighbour test and kernel factor.
+template <class T, int DIM, bool CONT, bool MOM>
 inline void sph_pair_loop(const CellList& cl, const SphState<T>& s, const SphConst<T>& k, const std::vector<T>& P,
                           size_t i, T* acc, T& drho) {
   T a[3] = {T(0.0), T(0.0), T(0.0)};
   T dr = T(0.0);
   const T xi[3] = {s.x[0][i], s.x[1][i], DIM == 3 ? s.x[2][i] : T(0.0)};
   const T vi[3] = {s.v[0][i], s.v[1][i], DIM == 3 ? s.v[2][i] : T(0.0)};
-  const T rhoi = s.rho[i], Pi = P[i];
+  const T rhoi = s.rho[i];
+  const T Pi = MOM ? P[i] : T(0.0);
   for_each_candidate(cl, cl.cell[i], [&](uint32_t j) {
     T d[3];
     for (int c = 0; c < DIM; ++c) d[c] = xi[c] - s.x[c][j];
@@ -354,17 +356,19 @@ inline void sph_pair_loop(const CellList& cl, const SphState<T>& s, const SphCon
     T w = dv[0] * d[0] + dv[1] * d[1];
     if (DIM == 3) w = w + dv[2] * d[2];
     const T mj = s.m[j];
-    dr = dr + mj * (w * F);
-    T pij = T(0.0);
-    if (value(w) < 0.0) pij = k.avk * w / ((r2 + k.eps_h2) * (rhoi + s.rho[j]));
-    const T coef = mj * (((Pi + P[j]) + pij) * F);
-    for (int c = 0; c < DIM; ++c) a[c] = a[c] - coef * d[c];
+    if (CONT) dr = dr + mj * (w * F);
+    if (MOM) {
+      T pij = T(0.0);
+      if (value(w) < 0.0) pij = k.avk * w / ((r2 + k.eps_h2) * (rhoi + s.rho[j]));
+      const T coef = mj * (((Pi + P[j]) + pij) * F);
+      for (int c = 0; c < DIM; ++c) a[c] = a[c] - coef * d[c];
+    }
   });
   for (int c = 0; c < 3; ++c) acc[c] = a[c];
   drho = dr;
 }
 
-// SPH rates (acc without gravity, drho) for all particles, arrays in id order.
+// SPH rates (acc without gravity, drho) of one state, all particles, arrays in id order.
 template <class T, int DIM>
 void sph_rates(const SphSpec& spec, const SphConst<T>& k, const SphState<T>& s, CellList& cl, std::vector<T>* acc,
                std::vector<T>& drho) {
@@ -378,16 +382,43 @@ void sph_rates(const SphSpec& spec, const SphConst<T>& k, const SphState<T>& s, 
 #pragma omp parallel for schedule(dynamic, 256)
   for (long long i = 0; i < (long long)s.n; ++i) {
     T a[3], dr;
-    sph_pair_loop<T, DIM>(cl, s, k, P, (size_t)i, a, dr);
+    sph_pair_loop<T, DIM, true, true>(cl, s, k, P, (size_t)i, a, dr);
     for (int c = 0; c < 3; ++c) acc[c][i] = a[c];
     drho[i] = dr;
   }
   (void)spec;
 }
 
+// One time step: symplectic Euler with the density advanced first.
+//   rho' = rho + dt C(x, v)                 C: continuity rate (all particles)
+//   v'   = v + dt (M(x, v, rho') + g)       M: momentum rate with the new densities (fluid)
+//   x'   = x + dt v'                        (fluid; wall particles keep x and v)
+// The acoustic pair (rho, v) is then advanced symplectically (stable for omega dt < 2); a
+// single evaluation of both rates from (x, v, rho) would advance it by forward Euler, which
+// amplifies every acoustic mode.
 template <class T, int DIM>
-void sph_integrate(const SphSpec& spec, const SphConst<T>& k, SphState<T>& s, const std::vector<T>* acc,
-                   const std::vector<T>& drho) {
+void sph_step(const SphSpec& spec, const SphConst<T>& k, SphState<T>& s, CellList& cl, std::vector<T>& P) {
+  const T* pos[3] = {s.x[0].data(), s.x[1].data(), DIM == 3 ? s.x[2].data() : s.x[0].data()};
+  build_cell_list<T>(cl, s.n, pos);
+  P.resize(s.n);
+  std::vector<T> rho_new(s.n);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long i = 0; i < (long long)s.n; ++i) {
+    T a[3], dr;
+    sph_pair_loop<T, DIM, true, false>(cl, s, k, P, (size_t)i, a, dr);
+    rho_new[i] = s.rho[i] + k.dt * dr;
+  }
+  s.rho.swap(rho_new);
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < (long long)s.n; ++i) P[i] = tait_pterm(k, s.rho[i]);
+  std::vector<T> acc[3];
+  for (int c = 0; c < DIM; ++c) acc[c].resize(s.n);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long i = 0; i < (long long)s.n; ++i) {
+    T a[3], dr;
+    sph_pair_loop<T, DIM, false, true>(cl, s, k, P, (size_t)i, a, dr);
+    for (int c = 0; c < DIM; ++c) acc[c][i] = a[c];
+  }
 #pragma omp parallel for schedule(static)
   for (long long i = 0; i < (long long)s.n; ++i) {
     if ((size_t)i < spec.n_fluid) {
@@ -396,7 +427,6 @@ void sph_integrate(const SphSpec& spec, const SphConst<T>& k, SphState<T>& s, co
         s.x[c][i] = s.x[c][i] + k.dt * s.v[c][i];
       }
     }
-    s.rho[i] = s.rho[i] + k.dt * drho[i];
   }
 }
 
@@ -404,11 +434,8 @@ template <class T, int DIM>
 void sph_run(const SphSpec& spec, const SphConst<T>& k, SphState<T>& s, int nsteps) {
   CellList cl;
   cl.g = make_grid(DIM, spec.lo, spec.hi, 2.0 * spec.h, spec.cell_mult);
-  std::vector<T> acc[3], drho;
-  for (int it = 0; it < nsteps; ++it) {
-    sph_rates<T, DIM>(spec, k, s, cl, acc, drho);
-    sph_integrate<T, DIM>(spec, k, s, acc, drho);
-  }
+  std::vector<T> P;
+  for (int it = 0; it < nsteps; ++it) sph_step<T, DIM>(spec, k, s, cl, P);
 }
 
 // ----------------------------------------------------------------------------------------

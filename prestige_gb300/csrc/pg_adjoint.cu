@@ -1,37 +1,41 @@
 // Reverse-mode differentiation of the SPH step (f64), with checkpointed recomputation.
 //
 // The reference has no differentiation; this is the adjoint of the forward step in pg_sph.cu
-// (continuity + Tait pressure + Monaghan viscosity as a gather into i over neighbours j, the
-// semantics of prestige/src/codegen/simple_cpu.rs:7-19, followed by the kick-drift update).
+// (continuity, Tait pressure and Monaghan viscosity as gathers into i over neighbours j, the
+// semantics of prestige/src/codegen/simple_cpu.rs:7-19, with the symplectic Euler update).
 //
 // Forward step t -> t+1 (fluid particles; wall particles keep x and v):
-//   v' = v + dt (a + g),  x' = x + dt v',  rho' = rho + dt drho
-// Given the adjoints (lx', lv', lr') of the state after the step, the adjoints before it are
-//   abar = dt (lv' + dt lx')   (fluid; 0 for walls),   dbar = dt lr'
-//   lx = lx' + dPhi/dx,  lv = (lv' + dt lx' | lv') + dPhi/dv,  lr = lr' + dPhi/drho
-// where Phi = sum_i (abar_i . a_i + dbar_i drho_i).  For one unordered pair (i, j) the two
-// ordered terms of Phi combine, because x_ji = -x_ij, v_ji = -v_ij and w, F, Pi_ij, P_i + P_j
-// are symmetric, into
-//   Lam = F (w D - S (x . E)),   D = dbar_i m_j + dbar_j m_i,   E = m_j abar_i - m_i abar_j,
-//   x = x_i - x_j,  v = v_i - v_j,  w = v . x,  S = P_i + P_j + Pi,  Pi = c1 w (w < 0, else 0),
-//   c1 = avk / ((r^2 + eps h^2)(rho_i + rho_j)),  F = (dW/dr)/r,  G = (dF/dr)/r
-// and its derivatives give particle i's share without any scatter:
-//   dLam/dx     = [G (w D - S xE) + 2 F xE Pi / (r^2 + eps h^2)] x + F (D - c1 xE) v - F S E
-//   dLam/dv     = F (D - c1 xE) x
-//   dLam/drho_i = -F xE (P'(rho_i) - Pi / (rho_i + rho_j))
-// with xE = x . E and P'(rho) = B ((gamma - 2)(rho/rho0)^gamma + 2) / rho^3.  Each thread
-// evaluates Lam for all its neighbours, so the transpose of the pair Jacobian is a second
-// gather over the same cell lists (no atomics, deterministic order).  The parameter
-// derivatives take only the ordered pair (i, j):
+//   rho' = rho + dt C(x, v),   v' = v + dt (M(x, v, rho') + g),   x' = x + dt v'
+// Given the adjoints (lx', lv', lr') of the state after the step:
+//   momentum adjoint    abar = dt (lv' + dt lx')  (fluid; 0 for walls)
+//                       Phi_M = sum_i abar_i . M_i,   lr'_tot = lr' + dPhi_M/drho'
+//   continuity adjoint  dbar = dt lr'_tot,  Phi_C = sum_i dbar_i C_i
+//   lx = lx' + dPhi_M/dx + dPhi_C/dx,   lv = (lv' + dt lx' | lv') + dPhi_M/dv + dPhi_C/dv,
+//   lr = lr'_tot (C does not depend on rho)
+// For one unordered pair (i, j) the two ordered terms of Phi combine, because x_ji = -x_ij,
+// v_ji = -v_ij and w, F, Pi_ij, P_i + P_j are symmetric, into
+//   Lam_M = -F S (x . E),  E = m_j abar_i - m_i abar_j,  S = P_i + P_j + Pi,  Pi = c1 w (w < 0)
+//   Lam_C =  F w D,        D = dbar_i m_j + dbar_j m_i
+//   x = x_i - x_j,  v = v_i - v_j,  w = v . x,  c1 = avk / ((r^2 + eps h^2)(rho_i + rho_j)),
+//   F = (dW/dr)/r,  G = (dF/dr)/r
+// whose derivatives give particle i's share without any scatter:
+//   dLam_M/dx = [-G S xE + 2 F xE Pi / (r^2 + eps h^2)] x - F c1 xE v - F S E,
+//   dLam_M/dv = -F c1 xE x,   dLam_M/drho_i = -F xE (P'(rho_i) - Pi / (rho_i + rho_j)),
+//   dLam_C/dx = G w D x + F D v,   dLam_C/dv = F D x
+// with xE = x . E and P'(rho) = B ((gamma - 2)(rho/rho0)^gamma + 2) / rho^3 (all densities
+// are rho', the ones the momentum rate used).  Each thread evaluates Lam for all its
+// neighbours, so the transpose of the pair Jacobian is a second gather over the same cell
+// lists (no atomics, deterministic order).  The parameter derivatives take only the ordered
+// pair (i, j) of Phi_M:
 //   dPhi/dalpha += -m_j F (abar_i . x) (-2 c0 h) w / ((r^2 + eps h^2)(rho_i + rho_j))  (w < 0)
 //   dPhi/dB     += -m_j F (abar_i . x) (P_i + P_j) / B
 // accumulated per particle and summed in a fixed order at the end.
 //
 // Checkpointing: pg_forward_checkpointed keeps the state every `every` steps.  pg_backward
 // walks the segments last to first; for each it restores the checkpoint, re-runs the forward
-// steps while keeping each step's state and its neighbour structure (sorted cells, sorted ids,
-// cell table: integer data, reused as is), then sweeps the adjoint back through the segment.
-// Memory: (nsteps / every) checkpoints plus one segment of `every` steps.
+// steps while keeping each step's state, its updated density and its neighbour structure
+// (sorted cells, sorted ids, cell table: integer data, reused as is), then sweeps the adjoint
+// back through the segment.  Memory: (nsteps / every) checkpoints plus one segment.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -52,13 +56,15 @@ struct pg_adjoint {
   pg::DevBuf ckpt;           // nseg states
   pg::DevBuf final_state;
   pg::DevBuf seg_state;      // `every` states of the segment being swept
+  pg::DevBuf seg_rnext;      // rho' of each step of the segment
   pg::DevBuf seg_cell, seg_id, seg_start;
   pg::DevBuf lx, lv, lr, ga, gb;
-  pg::DevBuf X4, V4, Q4, A4, PF;  // slot-ordered packs of one adjoint step
-  int pass_grid = 0;
+  pg::DevBuf X4, V4, Q4, A4, PF, DB;  // slot-ordered packs of one adjoint step
+  int pass_grid[3] = {0, 0, 0};
   size_t bytes() const {
-    const pg::DevBuf* b[] = {&ckpt, &final_state, &seg_state, &seg_cell, &seg_id, &seg_start, &lx, &lv,
-                             &lr,    &ga,          &gb,         &X4,       &V4,     &Q4,        &A4, &PF};
+    const pg::DevBuf* b[] = {&ckpt, &final_state, &seg_state, &seg_rnext, &seg_cell, &seg_id, &seg_start,
+                             &lx,   &lv,          &lr,        &ga,        &gb,       &X4,     &V4,
+                             &Q4,   &A4,          &PF,        &DB};
     size_t t = 0;
     for (const pg::DevBuf* d : b) t += d->bytes;
     return t;
@@ -78,8 +84,8 @@ namespace {
 
 using namespace sphpass;
 
-// Slot-ordered packs for one adjoint step:
-//   X4 {x, y, z, m}   V4 {vx, vy, vz, rho}   Q4 {P, P'(rho), P/B, dbar}   A4 {abar, 0}   PF float4 x
+// Slot-ordered packs for one adjoint step (a.rho points at rho' of the step):
+//   X4 {x, y, z, m}   V4 {vx, vy, vz, rho'}   Q4 {P, P'(rho'), P/B, 0}   A4 {abar, 0}   PF float4 x
 template <int DIM>
 __global__ void adjoint_prep_kernel(SphArgs a) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -90,7 +96,6 @@ __global__ void adjoint_prep_kernel(SphArgs a) {
   const double* vel = (const double*)a.vel;
   const double* lx = (const double*)a.lam[0];
   const double* lv = (const double*)a.lam[1];
-  const double* lr = (const double*)a.lam[2];
   const double rho = ((const double*)a.rho)[id];
   const double m = ((const double*)a.mass)[id];
   const double dt = K.d.dt;
@@ -112,14 +117,18 @@ __global__ void adjoint_prep_kernel(SphArgs a) {
   const double PB = (pw - 1.0) * inv_r2;
   ((double4_32a*)a.s[0])[k] = make_double4_32a(x[0], x[1], x[2], m);
   ((double4_32a*)a.s[1])[k] = make_double4_32a(v[0], v[1], v[2], rho);
-  ((double4_32a*)a.s[2])[k] = make_double4_32a(P, Pd, PB, dt * lr[id]);
+  ((double4_32a*)a.s[2])[k] = make_double4_32a(P, Pd, PB, 0.0);
   ((double4_32a*)a.s[3])[k] = make_double4_32a(ab[0], ab[1], ab[2], 0.0);
   ((float4*)a.s[4])[k] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
 }
 
-template <int DIM>
+// STAGE SPH_MOM: adjoint of the momentum rate (seeds abar); also writes dbar = dt lr'_tot into
+// the slot pack DB for the continuity adjoint.  STAGE SPH_CONT: adjoint of the continuity rate.
+template <int DIM, int STAGE>
 struct AdjPairs {
+  static constexpr bool kMom = STAGE == SPH_MOM;
   const double4_32a *X, *V, *Q, *A;
+  const double* DBp;
   double fa, fb, inv_h, four_h2, eps_h2, avk, avk_alpha;
   double xi[3], vi[3], ai[3], rhoi, mi, Pi, Pdi, PBi, dbi;
   double gx[3], gv[3], gr, gal, gB;
@@ -129,6 +138,7 @@ struct AdjPairs {
     V = (const double4_32a*)a.s[1];
     Q = (const double4_32a*)a.s[2];
     A = (const double4_32a*)a.s[3];
+    DBp = (const double*)a.s[5];
     fa = K.d.fa;
     fb = K.d.fb;
     inv_h = K.d.inv_h;
@@ -136,11 +146,18 @@ struct AdjPairs {
     eps_h2 = K.d.eps_h2;
     avk = K.d.avk;
     avk_alpha = K.avk_alpha;
-    const double4_32a x = X[k], v = V[k], q = Q[k], ab = A[k];
+    const double4_32a x = X[k], v = V[k];
     xi[0] = x.x; xi[1] = x.y; xi[2] = x.z; mi = x.w;
     vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; rhoi = v.w;
-    Pi = q.x; Pdi = q.y; PBi = q.z; dbi = q.w;
-    ai[0] = ab.x; ai[1] = ab.y; ai[2] = ab.z;
+    Pi = Pdi = PBi = dbi = 0.0;
+    ai[0] = ai[1] = ai[2] = 0.0;
+    if (kMom) {
+      const double4_32a q = Q[k], ab = A[k];
+      Pi = q.x; Pdi = q.y; PBi = q.z;
+      ai[0] = ab.x; ai[1] = ab.y; ai[2] = ab.z;
+    } else {
+      dbi = DBp[k];
+    }
     gx[0] = gx[1] = gx[2] = 0.0;
     gv[0] = gv[1] = gv[2] = 0.0;
     gr = gal = gB = 0.0;
@@ -153,8 +170,8 @@ struct AdjPairs {
     double r2 = __dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1]));
     if (DIM == 3) r2 = __dadd_rn(r2, __dmul_rn(d[2], d[2]));
     if (!(r2 < four_h2) || !(r2 > 0.0)) return;
-    const double4_32a vj = V[t], qj = Q[t], aj = A[t];
-    const double mj = xj.w, rhoj = vj.w;
+    const double4_32a vj = V[t];
+    const double mj = xj.w;
     const double r = sqrt(r2);
     const double inv_r = 1.0 / r;
     const double q = r * inv_h;
@@ -170,7 +187,18 @@ struct AdjPairs {
     const double dv[3] = {vi[0] - vj.x, vi[1] - vj.y, DIM == 3 ? vi[2] - vj.z : 0.0};
     double w = dv[0] * d[0] + dv[1] * d[1];
     if (DIM == 3) w += dv[2] * d[2];
-    const double rb = rhoi + rhoj;
+    if (!kMom) {
+      const double D = dbi * mj + DBp[t] * mi;
+      const double gw = G * w * D, fd = F * D;
+#pragma unroll
+      for (int c = 0; c < DIM; ++c) {
+        gx[c] += gw * d[c] + fd * dv[c];
+        gv[c] += fd * d[c];
+      }
+      return;
+    }
+    const double4_32a qj = Q[t], aj = A[t];
+    const double rb = rhoi + vj.w;
     const double e = r2 + eps_h2;
     double c1 = 0.0, c1a = 0.0;
     if (w < 0.0) {
@@ -180,7 +208,6 @@ struct AdjPairs {
     }
     const double PI = c1 * w;
     const double S = Pi + qj.x + PI;
-    const double D = dbi * mj + qj.w * mi;
     double E[3], xE = 0.0, axd = 0.0;
 #pragma unroll
     for (int c = 0; c < DIM; ++c) {
@@ -188,8 +215,8 @@ struct AdjPairs {
       xE += d[c] * E[c];
       axd += ai[c] * d[c];
     }
-    const double a1 = G * (w * D - S * xE) + 2.0 * F * xE * PI / e;
-    const double b1 = F * (D - c1 * xE);
+    const double a1 = -G * S * xE + 2.0 * F * xE * PI / e;
+    const double b1 = -F * c1 * xE;
     const double fs = F * S;
 #pragma unroll
     for (int c = 0; c < DIM; ++c) {
@@ -202,10 +229,19 @@ struct AdjPairs {
     gB -= own * (PBi + qj.z);
   }
 
-  __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id) {
+  __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id, uint32_t k) {
     double* lx = (double*)a.lam[0];
     double* lv = (double*)a.lam[1];
     double* lr = (double*)a.lam[2];
+    if (!kMom) {
+#pragma unroll
+      for (int c = 0; c < DIM; ++c) {
+        const size_t o = (size_t)id * DIM + c;
+        lx[o] += gx[c];
+        lv[o] += gv[c];
+      }
+      return;
+    }
     const bool fluid = id < K.fluid_end;
     const double dt = K.d.dt;
 #pragma unroll
@@ -215,7 +251,9 @@ struct AdjPairs {
       lx[o] = lxo + gx[c];
       lv[o] = (fluid ? lv[o] + dt * lxo : lv[o]) + gv[c];
     }
-    lr[id] += gr;
+    const double lrt = lr[id] + gr;
+    lr[id] = lrt;
+    ((double*)a.s[5])[k] = dt * lrt;
     ((double*)a.lam[3])[id] += gal;
     ((double*)a.lam[4])[id] += gB;
   }
@@ -232,23 +270,26 @@ int launch_adjoint_prep(cudaStream_t st, const SphArgs& a) {
   return PG_OK;
 }
 
-int launch_adjoint_pass(cudaStream_t st, const SphArgs& a, int grid) {
+typedef void (*AdjKernel)(SphArgs, int);
+
+AdjKernel adjoint_kernel(int dim, int stage) {
+  if (stage == SPH_MOM)
+    return dim == 2 ? sph_pass_kernel<AdjPairs<2, SPH_MOM>, 2, false> : sph_pass_kernel<AdjPairs<3, SPH_MOM>, 3, false>;
+  return dim == 2 ? sph_pass_kernel<AdjPairs<2, SPH_CONT>, 2, false> : sph_pass_kernel<AdjPairs<3, SPH_CONT>, 3, false>;
+}
+
+int launch_adjoint_pass(cudaStream_t st, const SphArgs& a, int stage, int grid) {
   if (a.n == 0) return PG_OK;
   const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
   if (grid <= 0 || (uint32_t)grid > ntiles) grid = (int)ntiles;
-  if (a.dim == 2) sph_pass_kernel<AdjPairs<2>, 2, false><<<grid, kSphThreads, 0, st>>>(a, 4);
-  else sph_pass_kernel<AdjPairs<3>, 3, false><<<grid, kSphThreads, 0, st>>>(a, 4);
+  adjoint_kernel(a.dim, stage)<<<grid, kSphThreads, 0, st>>>(a, 4);
   PG_CUDA_TRY(cudaGetLastError());
   return PG_OK;
 }
 
-int adjoint_pass_occupancy(int dim) {
+int adjoint_pass_occupancy(int dim, int stage) {
   int blocks = 0;
-  cudaError_t e =
-      dim == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sph_pass_kernel<AdjPairs<2>, 2, false>,
-                                                               kSphThreads, 0)
-               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sph_pass_kernel<AdjPairs<3>, 3, false>,
-                                                               kSphThreads, 0);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, adjoint_kernel(dim, stage), kSphThreads, 0);
   return e == cudaSuccess ? blocks : 0;
 }
 
@@ -337,6 +378,7 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
   const size_t ncp1 = s->ncells + 1;
   const int every = A->every;
   PG_TRY(A->seg_state.ensure(8 * A->state_doubles * every + 8));
+  PG_TRY(A->seg_rnext.ensure(8 * nn * every));
   PG_TRY(A->seg_cell.ensure(4 * nn * every));
   PG_TRY(A->seg_id.ensure(4 * nn * every));
   PG_TRY(A->seg_start.ensure(4 * ncp1 * every));
@@ -350,11 +392,12 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
   PG_TRY(A->Q4.ensure(32 * nn));
   PG_TRY(A->A4.ensure(32 * nn));
   PG_TRY(A->PF.ensure(16 * nn));
-  if (A->pass_grid == 0) {
+  PG_TRY(A->DB.ensure(8 * nn));
+  if (A->pass_grid[pg::SPH_MOM] == 0) {
     int dev = 0, sms = 0;
     PG_CUDA_TRY(cudaGetDevice(&dev));
     PG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    A->pass_grid = pg::adjoint_pass_occupancy(s->dim) * sms;
+    for (int st = pg::SPH_CONT; st <= pg::SPH_MOM; ++st) A->pass_grid[st] = pg::adjoint_pass_occupancy(s->dim, st) * sms;
   }
   if (nd) PG_CUDA_TRY(cudaMemcpyAsync(A->lx.p, dL_dx, 8 * nd, cudaMemcpyHostToDevice, s->stream));
   PG_CUDA_TRY(cudaMemsetAsync(A->lv.p, 0, 8 * nn * s->dim, s->stream));
@@ -368,7 +411,7 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
   a.s[2] = A->Q4.p;
   a.s[3] = A->A4.p;
   a.s[4] = A->PF.p;
-  a.s[5] = nullptr;
+  a.s[5] = A->DB.p;
   a.lam[0] = A->lx.p;
   a.lam[1] = A->lv.p;
   a.lam[2] = A->lr.p;
@@ -377,16 +420,14 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
 
   for (int seg = A->nseg - 1; seg >= 0; --seg) {
     const int steps = std::min(every, A->nsteps - seg * every);
-    // recompute the segment, keeping each step's state and neighbour structure
+    // recompute the segment, keeping each step's state, rho' and neighbour structure
     PG_TRY(pg::copy_state_in(s, A->ckpt.as<double>() + (size_t)seg * A->state_doubles));
     for (int t = 0; t < steps; ++t) {
       PG_TRY(pg::copy_state_out(s, A->seg_state.as<double>() + (size_t)t * A->state_doubles));
-      if (t + 1 < steps) {
-        PG_TRY(pg::enqueue_sph_step(s, false, 1, nullptr));
-      } else {
-        PG_TRY(pg::enqueue_neighbors(s));
-      }
+      PG_TRY(pg::enqueue_sph_step(s, false, 1, nullptr));
       if (n) {
+        PG_CUDA_TRY(cudaMemcpyAsync(A->seg_rnext.as<double>() + (size_t)t * n, s->rho.p, 8 * n,
+                                    cudaMemcpyDeviceToDevice, s->stream));
         PG_CUDA_TRY(cudaMemcpyAsync(A->seg_cell.as<uint32_t>() + (size_t)t * n, s->nw.sorted_cell, 4 * n,
                                     cudaMemcpyDeviceToDevice, s->stream));
         PG_CUDA_TRY(cudaMemcpyAsync(A->seg_id.as<uint32_t>() + (size_t)t * n, s->nw.sorted_id, 4 * n,
@@ -400,12 +441,13 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
       const double* st = A->seg_state.as<double>() + (size_t)t * A->state_doubles;
       a.pos = (void*)st;
       a.vel = (void*)(st + nd);
-      a.rho = (void*)(st + 2 * nd);
+      a.rho = (void*)(A->seg_rnext.as<double>() + (size_t)t * n);
       a.sorted_cell = A->seg_cell.as<uint32_t>() + (size_t)t * n;
       a.sorted_id = A->seg_id.as<uint32_t>() + (size_t)t * n;
       a.cell_start = A->seg_start.as<uint32_t>() + (size_t)t * ncp1;
       PG_TRY(pg::launch_adjoint_prep(s->stream, a));
-      PG_TRY(pg::launch_adjoint_pass(s->stream, a, A->pass_grid));
+      PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_MOM, A->pass_grid[pg::SPH_MOM]));
+      PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_CONT, A->pass_grid[pg::SPH_CONT]));
     }
   }
   PG_TRY(pg::copy_state_in(s, A->final_state.as<double>()));

@@ -188,8 +188,8 @@ int enqueue_neighbors(pg_system* s) {
 // Kernels enqueued by one neighbour search (hash, radix passes, cell count, scan).
 long long neighbor_launches(const pg_system* s) { return 1 + 3LL * s->nw.passes + 1 + (s->ncells ? 3 : 0); }
 
-// ev (optional): 4 events recorded at stage boundaries (start, after the neighbour search,
-// after the sorted gather, end).
+// ev (optional): 5 events recorded at stage boundaries (start, after the neighbour search,
+// after the sorted gather, after the continuity pass, end).
 int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[0], s->stream));
   PG_TRY(enqueue_neighbors(s));
@@ -197,9 +197,17 @@ int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
   SphArgs a = sph_args(s, integrate, rates);
   PG_TRY(launch_sph_gather(s->stream, a, s->arith));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[2], s->stream));
-  PG_TRY(launch_sph_pass(s->stream, a, s->arith, s->pass_grid));
-  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
-  s->launches += neighbor_launches(s) + 2;
+  if (rates) {
+    PG_TRY(launch_sph_pass(s->stream, a, s->arith, SPH_RATES, s->pass_grid[SPH_RATES]));
+    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
+    s->launches += neighbor_launches(s) + 2;
+  } else {
+    PG_TRY(launch_sph_pass(s->stream, a, s->arith, SPH_CONT, s->pass_grid[SPH_CONT]));
+    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
+    PG_TRY(launch_sph_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM]));
+    s->launches += neighbor_launches(s) + 3;
+  }
+  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
   return PG_OK;
 }
 
@@ -239,40 +247,45 @@ int enqueue_dem_step(pg_system* s, cudaEvent_t* ev) {
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[2], s->stream));
   PG_TRY(launch_dem_pass(s->stream, a));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
+  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
   s->launches += neighbor_launches(s) + 2;
   return PG_OK;
 }
 
-// Four events for one timed step, from the pool.
+constexpr int kStepEvents = 5;
+
+// Events for one timed step, from the pool.
 int timing_events(pg_system* s, cudaEvent_t** out) {
-  while (s->ev_pool.size() < 4) {
+  while (s->ev_pool.size() < kStepEvents) {
     cudaEvent_t e;
     PG_CUDA_TRY(cudaEventCreate(&e));
     s->ev_pool.push_back(e);
   }
-  for (int i = 0; i < 4; ++i) {
+  for (int i = 0; i < kStepEvents; ++i) {
     s->ev_pending.push_back(s->ev_pool.back());
     s->ev_pool.pop_back();
   }
-  *out = &s->ev_pending[s->ev_pending.size() - 4];
+  *out = &s->ev_pending[s->ev_pending.size() - kStepEvents];
   return PG_OK;
 }
 
 // Fold the pending step events into the accumulators (stream must be idle).
 int timing_collect(pg_system* s) {
-  for (size_t b = 0; b + 4 <= s->ev_pending.size(); b += 4) {
+  for (size_t b = 0; b + kStepEvents <= s->ev_pending.size(); b += kStepEvents) {
     cudaEvent_t* e = &s->ev_pending[b];
-    float t01, t12, t23;
+    float t01, t12, t23, t24;
     PG_CUDA_TRY(cudaEventElapsedTime(&t01, e[0], e[1]));
     PG_CUDA_TRY(cudaEventElapsedTime(&t12, e[1], e[2]));
     PG_CUDA_TRY(cudaEventElapsedTime(&t23, e[2], e[3]));
+    PG_CUDA_TRY(cudaEventElapsedTime(&t24, e[2], e[4]));
     s->tacc.neighbor_ms += t01;
     s->tacc.gather_ms += t12;
-    s->tacc.pass_ms += t23;
+    s->tacc.pass_ms += t24;
+    s->tacc.cont_ms += t23;
     s->tacc.steps += 1;
   }
   // region: first start -> last end of the pending batch, added to the running region total
-  if (s->ev_pending.size() >= 4) {
+  if (s->ev_pending.size() >= kStepEvents) {
     float reg;
     PG_CUDA_TRY(cudaEventElapsedTime(&reg, s->ev_pending.front(), s->ev_pending.back()));
     s->tacc.region_ms += reg;
@@ -298,7 +311,7 @@ int enqueue_step(pg_system* s) {
   }
   if (!ev && s->graph_enabled && s->graph_exec[0]) {
     PG_CUDA_TRY(cudaGraphLaunch(s->graph_exec[0], s->stream));
-    s->launches += neighbor_launches(s) + 2;
+    s->launches += neighbor_launches(s) + 3;
     return PG_OK;
   }
   return enqueue_sph_step(s, false, 1, ev);
@@ -368,8 +381,10 @@ int choose_pass_grid(pg_system* s) {
   int dev = 0, sms = 0;
   PG_CUDA_TRY(cudaGetDevice(&dev));
   PG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int occ = sph_pass_occupancy(s->arith, s->dim);
-  s->pass_grid = occ > 0 ? occ * sms : 0;  // persistent: one resident wave
+  for (int st = 0; st < 3; ++st) {
+    const int occ = sph_pass_occupancy(s->arith, s->dim, st);
+    s->pass_grid[st] = occ > 0 ? occ * sms : 0;  // persistent: one resident wave
+  }
   return PG_OK;
 }
 
@@ -982,7 +997,7 @@ int pg_get_info(pg_system* s, pg_info* info) {
   info->arith = s->arith;
   info->n_cells = (long long)s->ncells;
   info->reach = s->grids[0].reach;
-  info->pass_grid = s->pass_grid;
+  info->pass_grid = s->pass_grid[SPH_MOM];
   info->sort_passes = s->nw.passes;
   for (int d = 0; d < 3; ++d) {
     info->grid_n[d] = s->grids[0].n[d];

@@ -17,6 +17,13 @@ enum Arith {
 
 constexpr int kSphThreads = 128;
 
+// Stages of the SPH pair pass.
+enum SphStage {
+  SPH_RATES = 0,  // continuity and momentum rates of one state (pg_compute_rates)
+  SPH_CONT = 1,   // continuity rate, then rho' = rho + dt C (first pass of a step)
+  SPH_MOM = 2,    // momentum rate with rho', then v' and x' (second pass of a step)
+};
+
 // SPH constants of one system in one precision (formulas of the oracle's sph_consts).
 template <class R>
 struct SphC {
@@ -62,14 +69,14 @@ struct SphArgs {
 };
 
 int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith);
-int launch_sph_pass(cudaStream_t st, const SphArgs& a, int arith, int grid);
-int sph_pass_occupancy(int arith, int dim);
+int launch_sph_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid);
+int sph_pass_occupancy(int arith, int dim, int stage);
 
 // Adjoint of one SPH step (pg_adjoint.cu).  s[0..4] hold the slot-ordered packs written by
 // launch_adjoint_prep; pos/vel/rho/mass are the state before the step (id order).
 int launch_adjoint_prep(cudaStream_t st, const SphArgs& a);
-int launch_adjoint_pass(cudaStream_t st, const SphArgs& a, int grid);
-int adjoint_pass_occupancy(int dim);
+int launch_adjoint_pass(cudaStream_t st, const SphArgs& a, int stage, int grid);
+int adjoint_pass_occupancy(int dim, int stage);
 // Bytes per particle of the sorted packed arrays s[0..5] for an arithmetic mode.
 void sph_sorted_layout(int arith, size_t sizes[6]);
 

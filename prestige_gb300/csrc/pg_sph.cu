@@ -1,23 +1,28 @@
 // Weakly-compressible SPH on the cell list: continuity, Tait pressure, Monaghan artificial
-// viscosity and the kick-drift integrator, fused into one pass per step.
+// viscosity and the symplectic Euler integrator.
 //
 // The reference states a pairwise equation as a gather into particle i over partners j
 // (prestige/src/lib.rs:7-12 `force[i] += mass[j]`, executed by the loop of
-// prestige/src/codegen/simple_cpu.rs:7-19).  This pass is that gather for the SPH rates,
+// prestige/src/codegen/simple_cpu.rs:7-19).  These passes are that gather for the SPH rates,
 // with j restricted to the particles of the neighbour cells and r_ij < 2h:
-//   drho_i = sum_j m_j (v_ij . x_ij) F_ij
-//   a_i    = -sum_j m_j (P_i + P_j + Pi_ij) F_ij x_ij            (+ g in the integrator)
+//   C_i = drho_i = sum_j m_j (v_ij . x_ij) F_ij
+//   M_i = a_i    = -sum_j m_j (P_i + P_j + Pi_ij) F_ij x_ij           (+ g in the integrator)
 //   F = (dW/dr)/r of the cubic spline (support 2h), P = p/rho^2, p = B((rho/rho0)^gamma - 1)
 //   Pi_ij  = -2 alpha c0 h (v_ij.x_ij) / ((r^2 + eps h^2)(rho_i + rho_j))  if v_ij.x_ij < 0
 //
-// Kernel structure (one thread per target particle i, slot order):
+// One time step is two passes over the same neighbour structure:
+//   continuity pass  rho' = rho + dt C(x, v)   (writes rho' and P(rho') into the sorted pack)
+//   momentum pass    v' = v + dt (M(x, v, rho') + g),  x' = x + dt v'   (fluid particles)
+// Advancing the density first makes the acoustic pair (rho, v) symplectic; evaluating both
+// rates from one snapshot would advance it by forward Euler, which amplifies every acoustic
+// mode.  A third variant (pg_compute_rates) evaluates C and M of one state in one pass.
+//
+// Kernel structure (one thread per target particle i, slot order; pg_sph_pass.cuh):
 //   phase 1  every candidate of the 9 (2D: 3) neighbour rows is tested in FP32 against a
 //            conservative bound on r^2; passing slots are appended to a per-thread list in
-//            shared memory.  Lanes walk their own concatenated candidate sequence, so a warp
-//            loops max_lane(candidates) times rather than sum_rows(max_lane(row length)).
+//            shared memory.
 //   phase 2  when any lane's list is full (or all lanes are done) the warp evaluates the
-//            listed pairs: the exact neighbour test, then the pair terms.  Nearly all lanes
-//            are busy, instead of ~15% of them under a per-candidate branch.
+//            listed pairs: the exact neighbour test, then the pair terms.
 // Pairs are evaluated in the oracle's order (rows z, y ascending; slots ascending), so the
 // IEEE modes reproduce the oracle bit for bit.
 #include <cuda_runtime.h>
@@ -34,8 +39,17 @@ namespace {
 
 using namespace sphpass;
 
+template <class R> struct V2;
+template <> struct V2<double> { typedef double2 T; };
+template <> struct V2<float> { typedef float2 T; };
+
+template <class R> __device__ __forceinline__ typename V2<R>::T make2(R a, R b);
+template <> __device__ __forceinline__ double2 make2<double>(double a, double b) { return make_double2(a, b); }
+template <> __device__ __forceinline__ float2 make2<float>(float a, float b) { return make_float2(a, b); }
+
 // ---------------------------------------------------------------------------------------
 // Sorted gather: slot k <- particle sorted_id[k]; precomputes P = p / rho^2.
+//   IEEE modes:   s0 {x, y, z, m}   s1 {vx, vy, vz, 0}   s2 {rho, P}   (f64: s3 float4 x)
 // ---------------------------------------------------------------------------------------
 template <class Ops, int DIM>
 __global__ void sph_gather_real(SphArgs a) {
@@ -57,16 +71,23 @@ __global__ void sph_gather_real(SphArgs a) {
   }
   R4 A, B;
   A.x = x[0]; A.y = x[1]; A.z = x[2]; A.w = m;
-  B.x = v[0]; B.y = v[1]; B.z = v[2]; B.w = rho;
+  B.x = v[0]; B.y = v[1]; B.z = v[2]; B.w = R(0);
   ((R4*)a.s[0])[k] = A;
   ((R4*)a.s[1])[k] = B;
-  ((R*)a.s[2])[k] = tait_pterm<Ops>(consts<R>(K), K.gamma, rho);
+  ((typename V2<R>::T*)a.s[2])[k] = make2<R>(rho, tait_pterm<Ops>(consts<R>(K), K.gamma, rho));
   if (sizeof(R) == 8) ((float4*)a.s[3])[k] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
 }
 
 // Double-word copies for the f64 fast mode:
-//   s0 {x,y,z,m}.hi  s1 {x,y,z,m}.lo  s2 {vx,vy,vz,P}.hi  s3 {vx,vy,vz,P}.lo  s4 rho (hi,lo)
-//   s5 double {x,y,z} for the exact neighbour test near the cut-off.
+//   s0 {x,y,z,m}.hi  s1 {x,y,z,m}.lo  s2 {vx,vy,vz,0}.hi  s3 {vx,vy,vz,0}.lo
+//   s4 {rho.hi, rho.lo, P.hi, P.lo}   s5 double {x,y,z} for the exact neighbour test near the cut-off.
+__device__ __forceinline__ float4 df_pack_rho_p(double rho, double P) {
+  float4 r;
+  df_split(rho, &r.x, &r.y);
+  df_split(P, &r.z, &r.w);
+  return r;
+}
+
 template <int DIM>
 __global__ void sph_gather_df(SphArgs a) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -83,7 +104,6 @@ __global__ void sph_gather_df(SphArgs a) {
     x[c] = pos[(size_t)id * DIM + c];
     v[c] = vel[(size_t)id * DIM + c];
   }
-  const double P = tait_pterm<OpsD>(K.d, K.gamma, rho);
   float4 ah, al, bh, bl;
   df_split(x[0], &ah.x, &al.x);
   df_split(x[1], &ah.y, &al.y);
@@ -92,27 +112,30 @@ __global__ void sph_gather_df(SphArgs a) {
   df_split(v[0], &bh.x, &bl.x);
   df_split(v[1], &bh.y, &bl.y);
   df_split(v[2], &bh.z, &bl.z);
-  df_split(P, &bh.w, &bl.w);
-  float2 r;
-  df_split(rho, &r.x, &r.y);
+  bh.w = bl.w = 0.f;
   ((float4*)a.s[0])[k] = ah;
   ((float4*)a.s[1])[k] = al;
   ((float4*)a.s[2])[k] = bh;
   ((float4*)a.s[3])[k] = bl;
-  ((float2*)a.s[4])[k] = r;
+  ((float4*)a.s[4])[k] = df_pack_rho_p(rho, tait_pterm<OpsD>(K.d, K.gamma, rho));
   ((double4_32a*)a.s[5])[k] = make_double4_32a(x[0], x[1], x[2], 0.0);
 }
 
 // ---------------------------------------------------------------------------------------
-// Pair-term policies.
+// Pair-term policies.  STAGE: SPH_RATES (C and M of one state, written to acc/drho),
+// SPH_CONT (C, then rho' = rho + dt C into the canonical state and the sorted pack),
+// SPH_MOM (M with the packed rho', then the velocity and position update).
 // ---------------------------------------------------------------------------------------
-template <class Ops, int DIM, bool EXACT_TEST>
+template <class Ops, int DIM, bool EXACT_TEST, int STAGE>
 struct RealPairs {
   typedef typename Ops::R R;
   typedef typename V4<R>::T R4;
+  typedef typename V2<R>::T R2;
+  static constexpr bool kCont = STAGE != SPH_MOM;
+  static constexpr bool kMom = STAGE != SPH_CONT;
   const R4* A;
   const R4* B;
-  const R* P;
+  const R2* Q;
   SphC<R> c;
   R xi[3], vi[3], rhoi, Pi;
   R acc[3], dr;
@@ -120,13 +143,17 @@ struct RealPairs {
   __device__ __forceinline__ void begin(const SphArgs& a, const SphK& K, uint32_t k) {
     A = (const R4*)a.s[0];
     B = (const R4*)a.s[1];
-    P = (const R*)a.s[2];
+    Q = (const R2*)a.s[2];
     c = consts<R>(K);
     const R4 Ai = A[k], Bi = B[k];
     xi[0] = Ai.x; xi[1] = Ai.y; xi[2] = Ai.z;
     vi[0] = Bi.x; vi[1] = Bi.y; vi[2] = Bi.z;
-    rhoi = Bi.w;
-    Pi = P[k];
+    rhoi = Pi = R(0);
+    if (kMom) {
+      const R2 q = Q[k];
+      rhoi = q.x;
+      Pi = q.y;
+    }
     acc[0] = acc[1] = acc[2] = R(0);
     dr = R(0);
   }
@@ -142,7 +169,6 @@ struct RealPairs {
       if (!(r2 > R(0))) return;
     }
     const R4 Bj = B[t];
-    const R Pj = P[t];
     const R r = Ops::sqrt(r2);
     const R q = Ops::mul(r, c.inv_h);
     R F;
@@ -157,43 +183,47 @@ struct RealPairs {
     R w = Ops::add(Ops::mul(dv0, d0), Ops::mul(dv1, d1));
     if (DIM == 3) w = Ops::add(w, Ops::mul(dv2, d2));
     const R mj = Aj.w;
-    dr = Ops::add(dr, Ops::mul(mj, Ops::mul(w, F)));
-    R pij = R(0);
-    if (w < R(0)) pij = Ops::div(Ops::mul(c.avk, w), Ops::mul(Ops::add(r2, c.eps_h2), Ops::add(rhoi, Bj.w)));
-    const R coef = Ops::mul(mj, Ops::mul(Ops::add(Ops::add(Pi, Pj), pij), F));
-    acc[0] = Ops::sub(acc[0], Ops::mul(coef, d0));
-    acc[1] = Ops::sub(acc[1], Ops::mul(coef, d1));
-    if (DIM == 3) acc[2] = Ops::sub(acc[2], Ops::mul(coef, d2));
+    if (kCont) dr = Ops::add(dr, Ops::mul(mj, Ops::mul(w, F)));
+    if (kMom) {
+      const R2 qj = Q[t];
+      R pij = R(0);
+      if (w < R(0)) pij = Ops::div(Ops::mul(c.avk, w), Ops::mul(Ops::add(r2, c.eps_h2), Ops::add(rhoi, qj.x)));
+      const R coef = Ops::mul(mj, Ops::mul(Ops::add(Ops::add(Pi, qj.y), pij), F));
+      acc[0] = Ops::sub(acc[0], Ops::mul(coef, d0));
+      acc[1] = Ops::sub(acc[1], Ops::mul(coef, d1));
+      if (DIM == 3) acc[2] = Ops::sub(acc[2], Ops::mul(coef, d2));
+    }
   }
 
-  __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id) {
-    if (a.acc) {
+  __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id, uint32_t k) {
+    if (STAGE == SPH_RATES) {
 #pragma unroll
       for (int cc = 0; cc < DIM; ++cc) ((R*)a.acc)[(size_t)id * DIM + cc] = acc[cc];
       ((R*)a.drho)[id] = dr;
-    }
-    if (a.integrate) {
+    } else if (STAGE == SPH_CONT) {
+      R* rho = (R*)a.rho;
+      const R rn = Ops::add(rho[id], Ops::mul(c.dt, dr));
+      rho[id] = rn;
+      ((R2*)a.s[2])[k] = make2<R>(rn, tait_pterm<Ops>(c, K.gamma, rn));
+    } else if (id < K.fluid_end) {
       R* pos = (R*)a.pos;
       R* vel = (R*)a.vel;
-      R* rho = (R*)a.rho;
-      if (id < K.fluid_end) {
 #pragma unroll
-        for (int cc = 0; cc < DIM; ++cc) {
-          const size_t o = (size_t)id * DIM + cc;
-          const R v = Ops::add(vel[o], Ops::mul(c.dt, Ops::add(acc[cc], c.g[cc])));
-          vel[o] = v;
-          pos[o] = Ops::add(pos[o], Ops::mul(c.dt, v));
-        }
+      for (int cc = 0; cc < DIM; ++cc) {
+        const size_t o = (size_t)id * DIM + cc;
+        const R v = Ops::add(vel[o], Ops::mul(c.dt, Ops::add(acc[cc], c.g[cc])));
+        vel[o] = v;
+        pos[o] = Ops::add(pos[o], Ops::mul(c.dt, v));
       }
-      rho[id] = Ops::add(rho[id], Ops::mul(c.dt, dr));
     }
   }
 };
 
-template <int DIM>
+template <int DIM, int STAGE>
 struct DfPairs {
-  const float4 *Ah, *Al, *Bh, *Bl;
-  const float2* Rr;
+  static constexpr bool kCont = STAGE != SPH_MOM;
+  static constexpr bool kMom = STAGE != SPH_CONT;
+  const float4 *Ah, *Al, *Bh, *Bl, *RP;
   const double4_32a* Xd;
   SphDF w;
   double four_h2;
@@ -206,16 +236,19 @@ struct DfPairs {
     Al = (const float4*)a.s[1];
     Bh = (const float4*)a.s[2];
     Bl = (const float4*)a.s[3];
-    Rr = (const float2*)a.s[4];
+    RP = (const float4*)a.s[4];
     Xd = (const double4_32a*)a.s[5];
     w = K.w;
     four_h2 = K.d.four_h2;
     const float4 ah = Ah[k], al = Al[k], bh = Bh[k], bl = Bl[k];
-    const float2 rr = Rr[k];
     xi[0] = df_make(ah.x, al.x); xi[1] = df_make(ah.y, al.y); xi[2] = df_make(ah.z, al.z);
     vi[0] = df_make(bh.x, bl.x); vi[1] = df_make(bh.y, bl.y); vi[2] = df_make(bh.z, bl.z);
-    Pi = df_make(bh.w, bl.w);
-    rhoi = df_make(rr.x, rr.y);
+    rhoi = Pi = df_make(0.f, 0.f);
+    if (kMom) {
+      const float4 rp = RP[k];
+      rhoi = df_make(rp.x, rp.y);
+      Pi = df_make(rp.z, rp.w);
+    }
     const double4_32a xd = Xd[k];
     xid[0] = xd.x; xid[1] = xd.y; xid[2] = xd.z;
     acc[0] = acc[1] = acc[2] = df_make(0.f, 0.f);
@@ -265,55 +298,83 @@ struct DfPairs {
     df wv = df_add(df_mul(dv0, d0), df_mul(dv1, d1));
     if (DIM == 3) wv = df_add(wv, df_mul(df_sub(vi[2], df_make(bh.z, bl.z)), d2));
     const df mj = df_make(ah.w, al.w);
-    dr = df_add(dr, df_mul(mj, df_mul(wv, F)));
-    df pij = df_make(0.f, 0.f);
-    if (wv.hi < 0.f) {
-      const float2 rj = Rr[t];
-      const df den = df_mul(df_add(r2, df_make(w.eps_h2[0], w.eps_h2[1])), df_add(rhoi, df_make(rj.x, rj.y)));
-      pij = df_div(df_mul(df_make(w.avk[0], w.avk[1]), wv), den);
+    if (kCont) dr = df_add(dr, df_mul(mj, df_mul(wv, F)));
+    if (kMom) {
+      const float4 rpj = RP[t];
+      df pij = df_make(0.f, 0.f);
+      if (wv.hi < 0.f) {
+        const df den = df_mul(df_add(r2, df_make(w.eps_h2[0], w.eps_h2[1])), df_add(rhoi, df_make(rpj.x, rpj.y)));
+        pij = df_div(df_mul(df_make(w.avk[0], w.avk[1]), wv), den);
+      }
+      const df coef = df_mul(mj, df_mul(df_add(df_add(Pi, df_make(rpj.z, rpj.w)), pij), F));
+      acc[0] = df_sub(acc[0], df_mul(coef, d0));
+      acc[1] = df_sub(acc[1], df_mul(coef, d1));
+      if (DIM == 3) acc[2] = df_sub(acc[2], df_mul(coef, d2));
     }
-    const df coef = df_mul(mj, df_mul(df_add(df_add(Pi, df_make(bh.w, bl.w)), pij), F));
-    acc[0] = df_sub(acc[0], df_mul(coef, d0));
-    acc[1] = df_sub(acc[1], df_mul(coef, d1));
-    if (DIM == 3) acc[2] = df_sub(acc[2], df_mul(coef, d2));
   }
 
-  __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id) {
-    double ad[3];
+  __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id, uint32_t k) {
+    const SphC<double>& c = K.d;
+    if (STAGE == SPH_RATES) {
 #pragma unroll
-    for (int cc = 0; cc < 3; ++cc) ad[cc] = df_to_double(acc[cc]);
-    const double drd = df_to_double(dr);
-    if (a.acc) {
-#pragma unroll
-      for (int cc = 0; cc < DIM; ++cc) ((double*)a.acc)[(size_t)id * DIM + cc] = ad[cc];
-      ((double*)a.drho)[id] = drd;
-    }
-    if (a.integrate) {
+      for (int cc = 0; cc < DIM; ++cc) ((double*)a.acc)[(size_t)id * DIM + cc] = df_to_double(acc[cc]);
+      ((double*)a.drho)[id] = df_to_double(dr);
+    } else if (STAGE == SPH_CONT) {
+      double* rho = (double*)a.rho;
+      const double rn = __dadd_rn(rho[id], __dmul_rn(c.dt, df_to_double(dr)));
+      rho[id] = rn;
+      ((float4*)a.s[4])[k] = df_pack_rho_p(rn, tait_pterm<OpsD>(c, K.gamma, rn));
+    } else if (id < K.fluid_end) {
       double* pos = (double*)a.pos;
       double* vel = (double*)a.vel;
-      double* rho = (double*)a.rho;
-      const SphC<double>& c = K.d;
-      if (id < K.fluid_end) {
 #pragma unroll
-        for (int cc = 0; cc < DIM; ++cc) {
-          const size_t o = (size_t)id * DIM + cc;
-          const double v = __dadd_rn(vel[o], __dmul_rn(c.dt, __dadd_rn(ad[cc], c.g[cc])));
-          vel[o] = v;
-          pos[o] = __dadd_rn(pos[o], __dmul_rn(c.dt, v));
-        }
+      for (int cc = 0; cc < DIM; ++cc) {
+        const size_t o = (size_t)id * DIM + cc;
+        const double v = __dadd_rn(vel[o], __dmul_rn(c.dt, __dadd_rn(df_to_double(acc[cc]), c.g[cc])));
+        vel[o] = v;
+        pos[o] = __dadd_rn(pos[o], __dmul_rn(c.dt, v));
       }
-      rho[id] = __dadd_rn(rho[id], __dmul_rn(c.dt, drd));
     }
   }
 };
 
-template <class Pairs, int DIM, bool EXACT_PF>
-int launch_pass(cudaStream_t st, const SphArgs& a, int pf_index, int grid) {
-  if (a.n == 0) return PG_OK;
-  const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
-  if (grid <= 0 || (uint32_t)grid > ntiles) grid = (int)ntiles;
-  sph_pass_kernel<Pairs, DIM, EXACT_PF><<<grid, kSphThreads, 0, st>>>(a, pf_index);
-  return PG_OK;
+// ---------------------------------------------------------------------------------------
+// Launch plumbing: one table of kernel instantiations per (arith, dim, stage).
+// ---------------------------------------------------------------------------------------
+typedef void (*PassKernel)(SphArgs, int);
+
+template <int DIM, int STAGE>
+PassKernel pass_kernel_for(int arith, int* pf_index) {
+  switch (arith) {
+    case ARITH_F64_EXACT:
+      *pf_index = 3;
+      return sph_pass_kernel<RealPairs<OpsD, DIM, true, STAGE>, DIM, false>;
+    case ARITH_F64_DF:
+      *pf_index = 0;
+      return sph_pass_kernel<DfPairs<DIM, STAGE>, DIM, false>;
+    case ARITH_F32_EXACT:
+      *pf_index = 0;
+      return sph_pass_kernel<RealPairs<OpsF, DIM, false, STAGE>, DIM, true>;
+    case ARITH_F32_FAST:
+      *pf_index = 0;
+      return sph_pass_kernel<RealPairs<OpsFF, DIM, false, STAGE>, DIM, true>;
+    default:
+      return nullptr;
+  }
+}
+
+template <int DIM>
+PassKernel pass_kernel_dim(int arith, int stage, int* pf_index) {
+  switch (stage) {
+    case SPH_RATES: return pass_kernel_for<DIM, SPH_RATES>(arith, pf_index);
+    case SPH_CONT: return pass_kernel_for<DIM, SPH_CONT>(arith, pf_index);
+    case SPH_MOM: return pass_kernel_for<DIM, SPH_MOM>(arith, pf_index);
+    default: return nullptr;
+  }
+}
+
+PassKernel pass_kernel(int arith, int dim, int stage, int* pf_index) {
+  return dim == 2 ? pass_kernel_dim<2>(arith, stage, pf_index) : pass_kernel_dim<3>(arith, stage, pf_index);
 }
 
 }  // namespace
@@ -321,14 +382,14 @@ int launch_pass(cudaStream_t st, const SphArgs& a, int pf_index, int grid) {
 void sph_sorted_layout(int arith, size_t sz[6]) {
   for (int i = 0; i < 6; ++i) sz[i] = 0;
   switch (arith) {
-    case ARITH_F64_EXACT:  // double4_32a A, double4_32a B, double P, float4 prefilter positions
-      sz[0] = 32; sz[1] = 32; sz[2] = 8; sz[3] = 16;
+    case ARITH_F64_EXACT:  // double4 {x,m}, double4 {v,0}, double2 {rho,P}, float4 prefilter positions
+      sz[0] = 32; sz[1] = 32; sz[2] = 16; sz[3] = 16;
       break;
-    case ARITH_F64_DF:  // float4 A.hi, A.lo, B.hi, B.lo, float2 rho, double4_32a exact positions
-      sz[0] = 16; sz[1] = 16; sz[2] = 16; sz[3] = 16; sz[4] = 8; sz[5] = 32;
+    case ARITH_F64_DF:  // float4 A.hi, A.lo, V.hi, V.lo, float4 {rho, P} (hi, lo), double4 exact positions
+      sz[0] = 16; sz[1] = 16; sz[2] = 16; sz[3] = 16; sz[4] = 16; sz[5] = 32;
       break;
-    default:  // float4 A, float4 B, float P
-      sz[0] = 16; sz[1] = 16; sz[2] = 4;
+    default:  // float4 {x,m}, float4 {v,0}, float2 {rho,P}
+      sz[0] = 16; sz[1] = 16; sz[2] = 8;
       break;
   }
 }
@@ -362,65 +423,26 @@ int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith) {
   return PG_OK;
 }
 
-int launch_sph_pass(cudaStream_t st, const SphArgs& a, int arith, int grid) {
-  const int dim = a.dim;
-  int s = PG_OK;
-  switch (arith) {
-    case ARITH_F64_EXACT:
-      s = dim == 2 ? launch_pass<RealPairs<OpsD, 2, true>, 2, false>(st, a, 3, grid)
-                   : launch_pass<RealPairs<OpsD, 3, true>, 3, false>(st, a, 3, grid);
-      break;
-    case ARITH_F64_DF:
-      s = dim == 2 ? launch_pass<DfPairs<2>, 2, false>(st, a, 0, grid)
-                   : launch_pass<DfPairs<3>, 3, false>(st, a, 0, grid);
-      break;
-    case ARITH_F32_EXACT:
-      s = dim == 2 ? launch_pass<RealPairs<OpsF, 2, false>, 2, true>(st, a, 0, grid)
-                   : launch_pass<RealPairs<OpsF, 3, false>, 3, true>(st, a, 0, grid);
-      break;
-    case ARITH_F32_FAST:
-      s = dim == 2 ? launch_pass<RealPairs<OpsFF, 2, false>, 2, true>(st, a, 0, grid)
-                   : launch_pass<RealPairs<OpsFF, 3, false>, 3, true>(st, a, 0, grid);
-      break;
-    default:
-      set_error("unknown arithmetic mode %d", arith);
-      return PG_EINVAL;
+int launch_sph_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid) {
+  int pf = 0;
+  PassKernel kern = pass_kernel(arith, a.dim, stage, &pf);
+  if (!kern) {
+    set_error("unknown arithmetic mode %d or stage %d", arith, stage);
+    return PG_EINVAL;
   }
-  if (s != PG_OK) return s;
+  if (a.n == 0) return PG_OK;
+  const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
+  if (grid <= 0 || (uint32_t)grid > ntiles) grid = (int)ntiles;
+  kern<<<grid, kSphThreads, 0, st>>>(a, pf);
   PG_CUDA_TRY(cudaGetLastError());
   return PG_OK;
 }
 
-int sph_pass_occupancy(int arith, int dim) {
-  int blocks = 0;
-  cudaError_t e = cudaSuccess;
-  switch (arith) {
-    case ARITH_F64_EXACT:
-      e = dim == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                         &blocks, sph_pass_kernel<RealPairs<OpsD, 2, true>, 2, false>, kSphThreads, 0)
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                         &blocks, sph_pass_kernel<RealPairs<OpsD, 3, true>, 3, false>, kSphThreads, 0);
-      break;
-    case ARITH_F64_DF:
-      e = dim == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sph_pass_kernel<DfPairs<2>, 2, false>,
-                                                                   kSphThreads, 0)
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sph_pass_kernel<DfPairs<3>, 3, false>,
-                                                                   kSphThreads, 0);
-      break;
-    case ARITH_F32_EXACT:
-      e = dim == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                         &blocks, sph_pass_kernel<RealPairs<OpsF, 2, false>, 2, true>, kSphThreads, 0)
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                         &blocks, sph_pass_kernel<RealPairs<OpsF, 3, false>, 3, true>, kSphThreads, 0);
-      break;
-    default:
-      e = dim == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                         &blocks, sph_pass_kernel<RealPairs<OpsFF, 2, false>, 2, true>, kSphThreads, 0)
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                         &blocks, sph_pass_kernel<RealPairs<OpsFF, 3, false>, 3, true>, kSphThreads, 0);
-      break;
-  }
-  if (e != cudaSuccess) return 0;
+int sph_pass_occupancy(int arith, int dim, int stage) {
+  int pf = 0, blocks = 0;
+  PassKernel kern = pass_kernel(arith, dim, stage, &pf);
+  if (!kern) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, kSphThreads, 0) != cudaSuccess) return 0;
   return blocks;
 }
 

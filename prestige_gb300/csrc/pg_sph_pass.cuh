@@ -6,7 +6,7 @@
 // A `Pairs` policy provides
 //   begin(args, system, slot)   load the target's data
 //   pair(slot_j)                one candidate that passed the filter (repeats the exact test)
-//   finish(args, system, id)    write the target's results (id order)
+//   finish(args, system, id, k) write the target's results (id order; k = its slot)
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kSphThreads) sph_pass_kernel(SphArgs a, int pf
         if (done) break;
       }
     }
-    if (live) P.finish(a, K, id);
+    if (live) P.finish(a, K, id, k);
   }
 }
 

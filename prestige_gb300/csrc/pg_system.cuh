@@ -46,7 +46,7 @@ struct pg_system {
   pg::DevBuf sorted[6];
   pg::DevBuf spos;
   pg::DevBuf tmp, tmp2, tmp3, tmp4;
-  int pass_grid = 0;
+  int pass_grid[3] = {0, 0, 0};  // per SphStage
 
   // DEM contact history, id order, double buffered
   pg::DevBuf hpid[2], hxi[2];
