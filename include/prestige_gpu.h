@@ -134,6 +134,31 @@ int pg_count_neighbors(pg_system* sys, uint32_t* counts);
  * *total receives the entry count; PG_EOVERFLOW if it exceeds capacity. */
 int pg_get_neighbor_list(pg_system* sys, uint64_t* offsets, uint32_t* neighbors, size_t capacity, size_t* total);
 
+/* Cell list of n particles that allocates no device memory.  No counterpart in the reference:
+ * it exists for callers that cannot call cudaMalloc.  Some hosts give all device memory to an
+ * allocator of their own (a pool or caching allocator they must not go around).  Others run
+ * in loops where cudaMalloc's implicit device synchronisation is not acceptable.
+ *
+ * Computes the same neighbour search as pg_build_neighbors (cell hash, stable (cell, id) radix
+ * sort, cell-start table), bit for bit, for positions already on the device.
+ *   pos          device, n * dim doubles, id order (x0 y0 [z0] x1 ...)
+ *   grid         domain_lo/hi, support and cell_multiplier as in pg_config
+ *   sorted_cell  device, n u32: cell of each sorted slot
+ *   sorted_id    device, n u32: particle id of each sorted slot
+ *   cell_start   device, cell_start_capacity u32; receives n_cells + 1 entries
+ *   n_cells      optional host output: the grid's cell count (also set when the capacity is
+ *                too small, so a call with capacity 0 tells the caller how much to pass)
+ *   stream       a cudaStream_t, or NULL for the default stream; the call only enqueues work
+ * Scratch: a fixed device array compiled into the library, about 8.3 MB, held on every device
+ * that uses it until the process exits.  n is limited to 1,048,576 particles; larger n gives
+ * PG_EINVAL.  The first call on a device looks up the array's device address with
+ * cudaGetSymbolAddress; make that first call before any stream capture.  Every call shares the
+ * array, so calls whose GPU work overlaps (other streams, unordered host threads) race; order
+ * them on one stream. */
+int pg_cell_list_noalloc(const double* pos, size_t n, int dim, const double domain_lo[3], const double domain_hi[3],
+                         double support, double cell_multiplier, uint32_t* sorted_cell, uint32_t* sorted_id,
+                         uint32_t* cell_start, size_t cell_start_capacity, size_t* n_cells, void* stream);
+
 /* The body of the reference's eq1 (prestige/src/lib.rs:7-12, `force[i] += mass[j]`) run over
  * the neighbour set instead of all j:  dst[i] += sum_{j : |x_i - x_j| < support} src[j]
  * (j == i included).  dst and src name scalar double slices. */

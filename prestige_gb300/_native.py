@@ -89,6 +89,8 @@ SIGNATURES = {
     "pg_timing_read": (_I, [_P, ctypes.POINTER(PgTiming)]),
     "pg_memory_bytes": (_I, [_P, ctypes.POINTER(_SZ)]),
     "pg_get_info": (_I, [_P, ctypes.POINTER(PgInfo)]),
+    "pg_cell_list_noalloc": (_I, [_P, _SZ, _I, _P, _P, ctypes.c_double, ctypes.c_double, _P, _P, _P, _SZ,
+                                  ctypes.POINTER(_SZ), _P]),
     "pg_last_error": (_S, []),
 }
 

@@ -14,6 +14,8 @@
 // Input order is id order, and every pass is stable, so equal cells stay in id order.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "pg_internal.cuh"
 
 namespace pg {
@@ -293,4 +295,168 @@ int sort_and_table(cudaStream_t st, NbrWork& w) {
   return PG_OK;
 }
 
+// =========================================================================================
+// Cell list without device allocation (pg_cell_list_noalloc).
+//
+// The radix sort above needs scratch beyond its inputs and outputs: a second key/value buffer
+// for the ping-pong passes, the per-tile digit histograms and the digit totals.  Handles get
+// that scratch from cudaMalloc when they are created.  This variant takes it from one
+// file-scope device array instead, so a call allocates nothing.  Its size fixes the largest
+// system it accepts (kNoAllocMaxParticles).
+//
+// The array is shared by every call on a device and keeps the previous call's contents.
+// Nothing in it needs to start at zero: the hash writes every key, each histogram launch
+// writes every bin of its tiles, the digit scan writes every total.  Calls whose work
+// overlaps on the GPU (different streams, or different host threads without ordering) race
+// on it.
+// =========================================================================================
+namespace {
+
+constexpr size_t kNoAllocMaxParticles = 1u << 20;
+constexpr size_t kNoAllocMaxTiles = (kNoAllocMaxParticles + kSortTile - 1) / kSortTile;
+constexpr size_t kNoAllocKeysOff = 0;
+constexpr size_t kNoAllocValsOff = kNoAllocKeysOff + 4 * kNoAllocMaxParticles;
+constexpr size_t kNoAllocHistOff = kNoAllocValsOff + 4 * kNoAllocMaxParticles;
+constexpr size_t kNoAllocTotalOff = kNoAllocHistOff + 4 * kRadix * kNoAllocMaxTiles;
+constexpr size_t kNoAllocBytes = kNoAllocTotalOff + 4 * kRadix;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device.  The array's name in host code
+// is only a host-side stand-in, so the address is looked up once per device with that device
+// current and kept.
+int noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  PG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) {
+    set_error("device ordinal %d is beyond the %d devices the no-allocation cell list supports", dev,
+              kNoAllocMaxDevices);
+    return PG_EINVAL;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error("cudaGetSymbolAddress of the cell-list scratch failed: %s", cudaGetErrorString(e));
+      return PG_ECUDA;
+    }
+    g_noalloc_addr[dev] = p;
+  }
+  *out = (unsigned char*)g_noalloc_addr[dev];
+  return PG_OK;
+}
+
+// Cell index of every particle (f64 positions, id order), the same arithmetic as hash_kernel:
+// c_d = clamp(floor((x_d - lo_d) * inv), 0, n_d - 1), one IEEE subtraction then one product.
+struct NoAllocGrid {
+  double lo[3];
+  double inv;
+  int n[3];
+  int dim;
+};
+
+__global__ void noalloc_hash_kernel(NoAllocGrid g, const double* __restrict__ pos, uint32_t n,
+                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c[3] = {0, 0, 0};
+  for (int d = 0; d < g.dim; ++d) {
+    const double t = __dmul_rn(__dsub_rn(pos[(size_t)i * g.dim + d], g.lo[d]), g.inv);
+    c[d] = !(t >= 0.0) ? 0 : (t >= (double)g.n[d] ? g.n[d] - 1 : (int)t);
+  }
+  keys[i] = ((uint32_t)c[2] * (uint32_t)g.n[1] + (uint32_t)c[1]) * (uint32_t)g.n[0] + (uint32_t)c[0];
+  vals[i] = i;
+}
+
+// start[c] = first slot whose cell is >= c (c = 0 .. ncells), by binary search over the
+// sorted cells, so every entry is written without a count buffer.
+__global__ void noalloc_cell_start_kernel(const uint32_t* __restrict__ cell, uint32_t n, uint32_t ncells,
+                                          uint32_t* __restrict__ start) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c > ncells) return;
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = lo + (hi - lo) / 2;
+    if (cell[mid] < c) lo = mid + 1;
+    else hi = mid;
+  }
+  start[c] = lo;
+}
+
+}  // namespace
+
 }  // namespace pg
+
+extern "C" int pg_cell_list_noalloc(const double* pos, size_t n, int dim, const double domain_lo[3],
+                                    const double domain_hi[3], double support, double cell_multiplier,
+                                    uint32_t* sorted_cell, uint32_t* sorted_id, uint32_t* cell_start,
+                                    size_t cell_start_capacity, size_t* n_cells, void* stream) {
+  using namespace pg;
+  clear_error();
+  if (dim != 2 && dim != 3) {
+    set_error("dim must be 2 or 3 (got %d)", dim);
+    return PG_EINVAL;
+  }
+  if (!domain_lo || !domain_hi) {
+    set_error("null domain bounds");
+    return PG_EINVAL;
+  }
+  if (n > kNoAllocMaxParticles) {
+    set_error("%zu particles exceed the %zu-particle limit of the no-allocation cell list", n,
+              kNoAllocMaxParticles);
+    return PG_EINVAL;
+  }
+  Grid g;
+  PG_TRY(make_grid(dim, domain_lo, domain_hi, support, cell_multiplier, &g));
+  const uint64_t nc = g.ncells();
+  if (n_cells) *n_cells = (size_t)nc;
+  if (!cell_start || cell_start_capacity < nc + 1) {
+    set_error("cell_start needs %llu entries (capacity %zu)", (unsigned long long)(nc + 1), cell_start_capacity);
+    return PG_EINVAL;
+  }
+  if (n && (!pos || !sorted_cell || !sorted_id)) {
+    set_error("null position or output buffer");
+    return PG_EINVAL;
+  }
+  unsigned char* scratch = nullptr;
+  PG_TRY(noalloc_scratch(&scratch));
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n) {
+    uint32_t* tmp_keys = (uint32_t*)(scratch + kNoAllocKeysOff);
+    uint32_t* tmp_vals = (uint32_t*)(scratch + kNoAllocValsOff);
+    uint32_t* hist = (uint32_t*)(scratch + kNoAllocHistOff);
+    uint32_t* digit_total = (uint32_t*)(scratch + kNoAllocTotalOff);
+    const int passes = (bits_needed(nc ? nc - 1 : 0) + 7) / 8;
+    const int tiles = (int)((n + kSortTile - 1) / kSortTile);
+    // Ping-pong between the scratch pair and the caller's outputs, starting on the side that
+    // makes the last pass land in the outputs.
+    uint32_t* kbuf[2] = {tmp_keys, sorted_cell};
+    uint32_t* vbuf[2] = {tmp_vals, sorted_id};
+    int cur = (passes % 2 == 0) ? 1 : 0;
+    NoAllocGrid ng;
+    for (int d = 0; d < 3; ++d) {
+      ng.lo[d] = g.lo[d];
+      ng.n[d] = g.n[d];
+    }
+    ng.inv = 1.0 / g.cell;
+    ng.dim = dim;
+    noalloc_hash_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ng, pos, (uint32_t)n, kbuf[cur], vbuf[cur]);
+    for (int p = 0; p < passes; ++p) {
+      const int shift = 8 * p;
+      digit_hist_kernel<<<tiles, kSortThreads, 0, st>>>(kbuf[cur], n, shift, tiles, hist);
+      digit_scan_kernel<<<kRadix, kSortThreads, 0, st>>>(hist, tiles, digit_total);
+      digit_scatter_kernel<<<tiles, kSortThreads, 0, st>>>(kbuf[cur], vbuf[cur], kbuf[cur ^ 1], vbuf[cur ^ 1], n,
+                                                           shift, tiles, hist, digit_total);
+      cur ^= 1;
+    }
+  }
+  noalloc_cell_start_kernel<<<(unsigned)((nc + 1 + 255) / 256), 256, 0, st>>>(sorted_cell, (uint32_t)n, (uint32_t)nc,
+                                                                             cell_start);
+  PG_CUDA_TRY(cudaGetLastError());
+  return PG_OK;
+}
