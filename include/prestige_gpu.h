@@ -74,7 +74,8 @@ typedef struct pg_config {
   /* tuning */
   int block_size;     /* reserved (0) */
   int f64_mode;       /* pg_f64_mode */
-  int reserved;
+  int list_capacity;  /* SPH neighbour-list slots per particle (0: 128 in 3D, 64 in 2D); a particle with
+                         more neighbours is still handled exactly, by a slower continued walk */
 } pg_config;
 
 /* Read-only description of a handle. */

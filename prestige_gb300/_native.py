@@ -32,7 +32,7 @@ class PgConfig(ctypes.Structure):
         ("r_max", ctypes.c_double),
         ("wall_lo", _d3), ("wall_hi", _d3),
         ("contact_capacity", ctypes.c_int),
-        ("block_size", ctypes.c_int), ("f64_mode", ctypes.c_int), ("reserved", ctypes.c_int),
+        ("block_size", ctypes.c_int), ("f64_mode", ctypes.c_int), ("list_capacity", ctypes.c_int),
     ]
 
 

@@ -135,6 +135,9 @@ int ensure_sorted_buffers(pg_system* s) {
   const size_t n = s->n ? s->n : 1;
   for (int i = 0; i < 6; ++i)
     if (sz[i]) PG_TRY(s->sorted[i].ensure(sz[i] * n));
+  PG_TRY(s->nlist.ensure(4 * n * (size_t)s->list_cap));
+  PG_TRY(s->nlen.ensure(4 * n));
+  PG_TRY(s->nresume.ensure(8 * n));
   return PG_OK;
 }
 
@@ -157,6 +160,10 @@ SphArgs sph_args(pg_system* s, int integrate, bool rates) {
   a.acc = rates ? s->acc.p : nullptr;
   a.drho = rates ? s->drho.p : nullptr;
   a.integrate = integrate;
+  a.nlist = s->nlist.as<uint32_t>();
+  a.nlen = s->nlen.as<uint32_t>();
+  a.nresume = s->nresume.as<uint32_t>();
+  a.cap = (uint32_t)s->list_cap;
   return a;
 }
 
@@ -197,15 +204,16 @@ int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
   SphArgs a = sph_args(s, integrate, rates);
   PG_TRY(launch_sph_gather(s->stream, a, s->arith));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[2], s->stream));
+  PG_TRY(launch_sph_list(s->stream, a, s->arith, s->list_grid));
   if (rates) {
-    PG_TRY(launch_sph_pass(s->stream, a, s->arith, SPH_RATES, s->pass_grid[SPH_RATES]));
+    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_RATES, s->pass_grid[SPH_RATES]));
     if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
-    s->launches += neighbor_launches(s) + 2;
-  } else {
-    PG_TRY(launch_sph_pass(s->stream, a, s->arith, SPH_CONT, s->pass_grid[SPH_CONT]));
-    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
-    PG_TRY(launch_sph_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM]));
     s->launches += neighbor_launches(s) + 3;
+  } else {
+    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_CONT, s->pass_grid[SPH_CONT]));
+    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
+    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM]));
+    s->launches += neighbor_launches(s) + 4;
   }
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
   return PG_OK;
@@ -311,7 +319,7 @@ int enqueue_step(pg_system* s) {
   }
   if (!ev && s->graph_enabled && s->graph_exec[0]) {
     PG_CUDA_TRY(cudaGraphLaunch(s->graph_exec[0], s->stream));
-    s->launches += neighbor_launches(s) + 3;
+    s->launches += neighbor_launches(s) + 4;
     return PG_OK;
   }
   return enqueue_sph_step(s, false, 1, ev);
@@ -382,9 +390,11 @@ int choose_pass_grid(pg_system* s) {
   PG_CUDA_TRY(cudaGetDevice(&dev));
   PG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   for (int st = 0; st < 3; ++st) {
-    const int occ = sph_pass_occupancy(s->arith, s->dim, st);
+    const int occ = sph_list_occupancy(s->arith, s->dim, st);
     s->pass_grid[st] = occ > 0 ? occ * sms : 0;  // persistent: one resident wave
   }
+  const int locc = sph_list_occupancy(s->arith, s->dim, -1);
+  s->list_grid = locc > 0 ? locc * sms : 0;
   return PG_OK;
 }
 
@@ -566,6 +576,7 @@ void pg_config_default(pg_config* c) {
   c->contact_capacity = 16;
   c->block_size = 0;
   c->f64_mode = PG_F64_NATIVE;
+  c->list_capacity = 0;
 }
 
 static int create_common(const pg_config* cfgs, const size_t* counts, int nsys, pg_system** out) {
@@ -607,6 +618,11 @@ static int create_common(const pg_config* cfgs, const size_t* counts, int nsys, 
   s->dim = c0.dim;
   s->f64 = c0.precision == PG_F64;
   s->arith = arith_of(c0, s->f64);
+  if (c0.list_capacity < 0 || c0.list_capacity > 4096) {
+    pg::set_error("list_capacity must be in 0..4096 (got %d)", c0.list_capacity);
+    return PG_EINVAL;
+  }
+  s->list_cap = c0.list_capacity > 0 ? c0.list_capacity : (c0.dim == 2 ? 64 : 128);
   s->n = total;
   s->nsys = nsys;
   s->id_begin.assign(nsys + 1, 0);
@@ -976,6 +992,7 @@ int pg_memory_bytes(pg_system* s, size_t* bytes) {
                               &s->contacts, &s->err};
   for (const pg::DevBuf* d : bufs) b += d->bytes;
   for (int i = 0; i < 6; ++i) b += s->sorted[i].bytes;
+  b += s->nlist.bytes + s->nlen.bytes + s->nresume.bytes;
   for (auto& kv : s->user) b += kv.second->bytes;
   b += s->adjoint_bytes();
   *bytes = b;

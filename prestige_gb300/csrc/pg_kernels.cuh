@@ -65,12 +65,20 @@ struct SphArgs {
   void* drho;
   void* lam[5];              // adjoint (pg_adjoint.cu): lambda_x, lambda_v, lambda_rho, dL/dalpha and
                              // dL/dB partial sums, all id order
+  uint32_t* nlist;           // neighbour lists, slot order: nlist[k * cap + q] (q < min(nlen[k], cap))
+  uint32_t* nlen;            // neighbours of slot k that passed the prefilter (may exceed cap)
+  uint32_t* nresume;         // (row, slot) where the walk continues when nlen[k] > cap
+  uint32_t cap;
   int integrate;
 };
 
 int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith);
 int launch_sph_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid);
 int sph_pass_occupancy(int arith, int dim, int stage);
+// Neighbour lists for the list-based passes (stage passes read a.nlist / a.nlen / a.nresume).
+int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid);
+int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid);
+int sph_list_occupancy(int arith, int dim, int stage);  // stage < 0: the list kernel
 
 // Adjoint of one SPH step (pg_adjoint.cu).  s[0..4] hold the slot-ordered packs written by
 // launch_adjoint_prep; pos/vel/rho/mass are the state before the step (id order).

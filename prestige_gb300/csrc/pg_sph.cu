@@ -377,6 +377,68 @@ PassKernel pass_kernel(int arith, int dim, int stage, int* pf_index) {
   return dim == 2 ? pass_kernel_dim<2>(arith, stage, pf_index) : pass_kernel_dim<3>(arith, stage, pf_index);
 }
 
+// The same table for the list-based passes and the list kernel (stage < 0).
+template <int DIM, int STAGE>
+PassKernel list_pass_for(int arith, int* pf_index) {
+  switch (arith) {
+    case ARITH_F64_EXACT:
+      *pf_index = 3;
+      return sph_list_pass_kernel<RealPairs<OpsD, DIM, true, STAGE>, DIM, false>;
+    case ARITH_F64_DF:
+      *pf_index = 0;
+      return sph_list_pass_kernel<DfPairs<DIM, STAGE>, DIM, false>;
+    case ARITH_F32_EXACT:
+      *pf_index = 0;
+      return sph_list_pass_kernel<RealPairs<OpsF, DIM, false, STAGE>, DIM, true>;
+    case ARITH_F32_FAST:
+      *pf_index = 0;
+      return sph_list_pass_kernel<RealPairs<OpsFF, DIM, false, STAGE>, DIM, true>;
+    default:
+      return nullptr;
+  }
+}
+
+template <int DIM>
+PassKernel list_kernel_dim(int arith, int stage, int* pf_index) {
+  switch (stage) {
+    case SPH_RATES: return list_pass_for<DIM, SPH_RATES>(arith, pf_index);
+    case SPH_CONT: return list_pass_for<DIM, SPH_CONT>(arith, pf_index);
+    case SPH_MOM: return list_pass_for<DIM, SPH_MOM>(arith, pf_index);
+    default: break;
+  }
+  switch (arith) {  // the list kernel
+    case ARITH_F64_EXACT:
+      *pf_index = 3;
+      return sph_list_kernel<DIM, false>;
+    case ARITH_F64_DF:
+      *pf_index = 0;
+      return sph_list_kernel<DIM, false>;
+    case ARITH_F32_EXACT:
+    case ARITH_F32_FAST:
+      *pf_index = 0;
+      return sph_list_kernel<DIM, true>;
+    default:
+      return nullptr;
+  }
+}
+
+PassKernel list_kernel(int arith, int dim, int stage, int* pf_index) {
+  return dim == 2 ? list_kernel_dim<2>(arith, stage, pf_index) : list_kernel_dim<3>(arith, stage, pf_index);
+}
+
+int launch_table(cudaStream_t st, const SphArgs& a, PassKernel kern, int pf, int grid) {
+  if (!kern) {
+    set_error("unknown arithmetic mode or stage");
+    return PG_EINVAL;
+  }
+  if (a.n == 0) return PG_OK;
+  const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
+  if (grid <= 0 || (uint32_t)grid > ntiles) grid = (int)ntiles;
+  kern<<<grid, kSphThreads, 0, st>>>(a, pf);
+  PG_CUDA_TRY(cudaGetLastError());
+  return PG_OK;
+}
+
 }  // namespace
 
 void sph_sorted_layout(int arith, size_t sz[6]) {
@@ -436,6 +498,26 @@ int launch_sph_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int
   kern<<<grid, kSphThreads, 0, st>>>(a, pf);
   PG_CUDA_TRY(cudaGetLastError());
   return PG_OK;
+}
+
+int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid) {
+  int pf = 0;
+  PassKernel kern = list_kernel(arith, a.dim, -1, &pf);
+  return launch_table(st, a, kern, pf, grid);
+}
+
+int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid) {
+  int pf = 0;
+  PassKernel kern = list_kernel(arith, a.dim, stage, &pf);
+  return launch_table(st, a, kern, pf, grid);
+}
+
+int sph_list_occupancy(int arith, int dim, int stage) {
+  int pf = 0, blocks = 0;
+  PassKernel kern = list_kernel(arith, dim, stage, &pf);
+  if (!kern) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, kSphThreads, 0) != cudaSuccess) return 0;
+  return blocks;
 }
 
 int sph_pass_occupancy(int arith, int dim, int stage) {

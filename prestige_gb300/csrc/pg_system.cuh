@@ -47,6 +47,9 @@ struct pg_system {
   pg::DevBuf spos;
   pg::DevBuf tmp, tmp2, tmp3, tmp4;
   int pass_grid[3] = {0, 0, 0};  // per SphStage
+  int list_grid = 0;
+  int list_cap = 128;            // neighbour-list slots per particle
+  pg::DevBuf nlist, nlen, nresume;
 
   // DEM contact history, id order, double buffered
   pg::DevBuf hpid[2], hxi[2];

@@ -155,3 +155,29 @@ def test_errors_are_reported(pg):
     assert e.value.status == nat.PG_ENOTFOUND
     with pytest.raises(nat.PgError):
         ParticleSystem(make_config(dim=4), 10)
+
+
+@pytest.mark.parametrize("cap", [4, 16])
+@pytest.mark.parametrize("precision,mode", [(1, 0), (0, 0), (1, 1)])
+def test_list_overflow_continues_the_walk(pg, oracle, cap, precision, mode):
+    """Neighbour lists shorter than the neighbour count: the pair passes finish the candidate
+    walk from where the list stopped, in the same order, so results are unchanged."""
+    w = workloads.sph_lattice_3d(n=3000, seed=21)
+    cfg = dict(w["config"])
+    cfg.update(precision=precision, f64_mode=mode, list_capacity=cap)
+    s = ParticleSystem(make_config(**cfg), w["n"])
+    f64 = precision == 1
+    dt = np.float64 if f64 else np.float32
+    for k in ("pos", "vel", "rho", "mass"):
+        s.set(k, np.asarray(w["fields"][k], dt))
+    acc, drho = s.compute_rates()
+    oacc, odrho = oracle.sph_rates(cfg, _ostate(oracle, w, f64=f64))
+    st = _ostate(oracle, w, f64=f64)
+    s.step(2)
+    oracle.sph_run(cfg, st, 2)
+    if mode == 0:
+        assert np.array_equal(acc, oacc) and np.array_equal(drho, odrho)
+        assert np.array_equal(s.get("pos"), st.pos) and np.array_equal(s.get("rho"), st.rho)
+    else:
+        assert _rel(acc, oacc) <= F64_TOL and _rel(drho, odrho) <= F64_TOL
+        assert _rel(s.get("pos"), st.pos) <= F64_TOL
