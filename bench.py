@@ -9,7 +9,11 @@ needed between steps.
 
 Output: one JSON line (rank 0).  `value` = particle-steps/s over the timed steps with the state
 resident in HBM (CUDA events on the library's stream, max over ranks); `e2e` = the same metric
-through the public C ABI with host buffers (pinned) copied in and out every step.
+through the public C ABI with host buffers (pinned) copied in and out every step.  `roofline`
+describes the momentum pass (the step's dominant kernel).  Unless --no-extras, three more
+sections on rank 0: `batched` (512 uneven 2D dam breaks in one handle vs looping the plain
+handles), `adjoint` (backward / forward cost of the differentiable 3D workload) and `dem`
+(200,000-sphere settling).
 
 `--impl reference` times the CPU path on the host cores instead: the reference has no executable
 particle path (its code generator returns text, prestige/src/codegen/simple_cpu.rs:3-22), so the
@@ -33,13 +37,13 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# Algorithmic bytes per particle of the pair pass (f64): reads pos, vel, rho, m once (64 B),
-# writes acc-equivalent state update and drho once (32 B).
-PASS_BYTES_F64 = 96
-PASS_BYTES_F32 = 48
-# DRAM bytes per particle per pass launch measured by ncu on the 1,000,000-particle lattice
-# (dram__bytes_read.sum + dram__bytes_write.sum of the pass kernel / N); see profiles/.
-PASS_TRAFFIC_PER_PARTICLE = None
+# Algorithmic bytes per particle of the momentum pass (the step's dominant kernel): reads
+# pos, vel, rho', m once and writes pos, vel once.  3D f64: 64 + 48 = 112 B; f32: 56 B.
+MOM_BYTES = {"f64": 112, "f32": 56}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per particle of one momentum-pass
+# launch, from the ncu capture summarised in profiles/sph_mom_pass_lattice3d.md (1,000,000
+# particles, f64 double-word mode), scaled by the particle count.
+MOM_TRAFFIC_PER_PARTICLE = {"f64-fast": None}
 
 METRIC = "particle-steps/s"
 
@@ -56,6 +60,7 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--cpu-sample-n", type=int, default=0, help="particles in the CPU-baseline sample (0: auto)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true", help="skip the batched, adjoint and DEM sections")
     return p.parse_args()
 
 
@@ -203,6 +208,113 @@ def run_reference(args, rank, world, pgroup):
     print(json.dumps(out), flush=True)
 
 
+def _peak_hbm():
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def bench_batched(steps=20, looped_steps=5):
+    """512 independent 2D dam breaks: one batched handle (graph-replayed step) against looping
+    the plain per-system handles (each also graph-replayed) over the same systems."""
+    import torch
+
+    from prestige_gb300 import ParticleSystem, workloads
+    systems = workloads.batched_dam_breaks()
+    total = sum(w["n"] for w in systems)
+    cfgs = [dict(w["config"], f64_mode=1) for w in systems]
+    b = ParticleSystem.batch(cfgs, [w["n"] for w in systems])
+    for k in ("pos", "vel", "rho", "mass"):
+        b.set(k, np.concatenate([w["fields"][k] for w in systems]))
+    b.enable_graph(True)
+    b.step(3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.step(steps)
+    tb = time.perf_counter() - t0
+    b.close()
+    hs = []
+    for w, c in zip(systems, cfgs):
+        h = ParticleSystem(c, w["n"])
+        workloads.load_into(h, w)
+        h.enable_graph(True)
+        hs.append(h)
+    for h in hs:
+        h.step_async(2)
+    for h in hs:
+        h.sync()
+    t0 = time.perf_counter()
+    for _ in range(looped_steps):
+        for h in hs:
+            h.step_async(1)
+    for h in hs:
+        h.sync()
+    tl = time.perf_counter() - t0
+    for h in hs:
+        h.close()
+    vb = total * steps / tb
+    vl = total * looped_steps / tl
+    return {"workload": "512 independent 2D dam breaks, N_i log-uniform in [500, 50000] (seed 3), H_i in "
+                        "[0.5, 2.0] m, per-system dx/h/c0/dt, f64 double-word mode",
+            "systems": len(systems), "particles": total, "batched_value": vb, "looped_value": vl,
+            "unit": "particle-steps/s", "batched_ms_per_step": 1e3 * tb / steps,
+            "looped_ms_per_step": 1e3 * tl / looped_steps, "batched_over_looped": vb / vl,
+            "timing": "host wall clock around graph-replayed steps, stream synchronised"}
+
+
+def bench_adjoint(nsteps=500, every=50, n=100000):
+    """Differentiable 3D SPH: forward with checkpoints, then the adjoint sweep (recompute +
+    adjoint passes); cost of a backward step over a forward step."""
+    import torch
+
+    from prestige_gb300 import ParticleSystem, make_config, workloads
+    w = workloads.differentiable_3d(n=n)
+    out = {"workload": "100,000-particle jittered lattice, 8 Fourier velocity modes (0.05 m/s), loss = mean "
+                       "squared distance to a seeded target, %d steps, checkpoints every %d" % (nsteps, every)}
+    for mode, name in ((0, "native"), (1, "fast")):
+        s = ParticleSystem(make_config(**dict(w["config"], f64_mode=mode)), n)
+        workloads.load_into(s, w)
+        s.step(3)
+        workloads.load_into(s, w)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.forward_checkpointed(nsteps, every)
+        tf = time.perf_counter() - t0
+        x = s.get("pos")
+        g = 2.0 * (x - w["target"]) / n
+        t0 = time.perf_counter()
+        da, dB, _ = s.backward(g)
+        tb = time.perf_counter() - t0
+        s.close()
+        out[name] = {"forward_ms_per_step": 1e3 * tf / nsteps, "backward_ms_per_step": 1e3 * tb / nsteps,
+                     "backward_over_forward": tb / tf, "dL_dalpha": da, "dL_dB": dB}
+    return out
+
+
+def bench_dem(steps=30):
+    """3D DEM settling, 200,000 spheres: particle-steps/s of the full step (graph-replayed)."""
+    import torch
+
+    from prestige_gb300 import ParticleSystem, workloads
+    w = workloads.dem_settling(200000)
+    s = ParticleSystem(w["config"], w["n"])
+    workloads.load_into(s, w)
+    s.enable_graph(True)
+    s.step(3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.step(steps)
+    t = time.perf_counter() - t0
+    contacts = s.dem_contacts()
+    s.close()
+    return {"workload": "200,000 spheres, r in [0.5, 1.0] mm, random sequential insertion in 0.1 x 0.1 x 0.3 m, "
+                        "kn 1e5, e 0.9, mu 0.3, dt 1e-6, f64", "particles": w["n"], "steps": steps,
+            "value": w["n"] * steps / t, "unit": "particle-steps/s", "ms_per_step": 1e3 * t / steps,
+            "contacts_last_step": contacts}
+
+
 def run_gpu(args, rank, world, local, pgroup):
     import torch
 
@@ -231,15 +343,15 @@ def run_gpu(args, rank, world, local, pgroup):
     region_ms = allmax(pgroup, t["region_ms"])
     ms_per_step = region_ms / args.steps
     value = world * n * args.steps / (region_ms * 1e-3)
-    pass_ms = t["pass_ms"] / args.steps
-    bpp = PASS_BYTES_F64 if args.precision == "f64" else PASS_BYTES_F32
-    achieved = bpp * n / (pass_ms * 1e-3) / 1e9
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    peak, peak_src = 6800.0, "fallback"
-    if os.path.exists(peaks_path):
-        with open(peaks_path) as f:
-            peak, peak_src = float(json.load(f)["hbm_gbs"]), "measured"
-    traffic = PASS_TRAFFIC_PER_PARTICLE * n if PASS_TRAFFIC_PER_PARTICLE else None
+    K = args.steps
+    list_ms = t["list_ms"] / K
+    cont_ms = t["cont_ms"] / K
+    mom_ms = (t["pass_ms"] - t["list_ms"] - t["cont_ms"]) / K
+    bpp = MOM_BYTES[args.precision]
+    achieved = bpp * n / (mom_ms * 1e-3) / 1e9
+    peak, peak_src = _peak_hbm()
+    tpp = MOM_TRAFFIC_PER_PARTICLE.get("%s-%s" % (args.precision, args.mode))
+    traffic = tpp * n if tpp else None
 
     # ---- end to end through the C ABI with pinned host buffers ----
     eb = 8 if args.precision == "f64" else 4
@@ -272,7 +384,7 @@ def run_gpu(args, rank, world, local, pgroup):
     barrier(pgroup)
     e2e_s = allmax(pgroup, e2e_s)
     e2e_value = world * n * args.e2e_steps / e2e_s
-    nbr_mean = None
+    s.close()
 
     if rank == 0:
         cpu = None
@@ -294,18 +406,23 @@ def run_gpu(args, rank, world, local, pgroup):
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "kernel": "sph_pass_kernel",
-                         "peak_source": peak_src,
-                         "bytes_per_particle": bpp},
-            "stages_ms_per_step": {"neighbor_search": t["neighbor_ms"] / args.steps,
-                                   "sorted_gather": t["gather_ms"] / args.steps, "pair_pass": pass_ms},
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "sph_list_pass_kernel (momentum pass)", "peak_source": peak_src,
+                         "bytes_per_particle": bpp,
+                         "binding_resource": "FP32 issue (double-word f64 arithmetic)" if args.mode == "fast"
+                         and args.precision == "f64" else ("FP64 pipe" if args.precision == "f64" else "FP32 issue")},
+            "stages_ms_per_step": {"neighbor_search": t["neighbor_ms"] / K, "sorted_gather": t["gather_ms"] / K,
+                                   "neighbor_lists": list_ms, "continuity_pass": cont_ms, "momentum_pass": mom_ms},
             "gpu_launches": int(t["launches"]),
             "clocks": clk,
             "cpu_baseline": cpu,
             "info": {"n_cells": info["n_cells"], "sort_passes": info["sort_passes"], "pass_grid": info["pass_grid"]},
         }
+        if not args.no_extras:
+            out["batched"] = bench_batched()
+            out["adjoint"] = bench_adjoint()
+            out["dem"] = bench_dem()
         print(json.dumps(out), flush=True)
-    s.close()
 
 
 def main():

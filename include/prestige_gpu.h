@@ -202,7 +202,8 @@ int pg_backward(pg_system* sys, const double* dL_dx, double* dL_dalpha, double* 
 int pg_autotune(pg_system* sys, int trial_steps, int* best_block, double* best_multiplier, int* best_f64_mode,
                 double* best_ms_per_step);
 
-/* Device-side timing of steps (CUDA events on the handle's stream).  pg_timing_enable(1) resets
+/* Device-side timing of steps (CUDA events on the handle's stream).  The momentum pass time is
+ * pass_ms - list_ms - cont_ms.  pg_timing_enable(1) resets
  * the accumulators and makes every later step record events around its stages (steps then run
  * eagerly, not from a graph); pg_timing_read waits for the stream and returns the totals since the
  * last enable. */
@@ -210,10 +211,11 @@ typedef struct pg_timing {
   double region_ms;    /* first timed step start -> last timed step end */
   double neighbor_ms;  /* hash + sort + cell table, summed over steps */
   double gather_ms;    /* sorted copies, summed */
-  double pass_ms;      /* pair passes + integrator, summed */
+  double pass_ms;      /* neighbour lists + pair passes + integrator (DEM: contact pass), summed */
   long long steps;
   long long launches;  /* kernels launched by the timed steps */
   double cont_ms;      /* SPH continuity pass alone (part of pass_ms), summed */
+  double list_ms;      /* SPH neighbour-list kernel alone (part of pass_ms), summed */
 } pg_timing;
 int pg_timing_enable(pg_system* sys, int enable);
 int pg_timing_read(pg_system* sys, pg_timing* out);

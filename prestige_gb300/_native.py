@@ -50,7 +50,7 @@ class PgInfo(ctypes.Structure):
 class PgTiming(ctypes.Structure):
     _fields_ = [("region_ms", ctypes.c_double), ("neighbor_ms", ctypes.c_double), ("gather_ms", ctypes.c_double),
                 ("pass_ms", ctypes.c_double), ("steps", ctypes.c_longlong), ("launches", ctypes.c_longlong),
-                ("cont_ms", ctypes.c_double)]
+                ("cont_ms", ctypes.c_double), ("list_ms", ctypes.c_double)]
 
 
 _P = ctypes.c_void_p

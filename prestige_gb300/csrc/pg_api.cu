@@ -195,8 +195,8 @@ int enqueue_neighbors(pg_system* s) {
 // Kernels enqueued by one neighbour search (hash, radix passes, cell count, scan).
 long long neighbor_launches(const pg_system* s) { return 1 + 3LL * s->nw.passes + 1 + (s->ncells ? 3 : 0); }
 
-// ev (optional): 5 events recorded at stage boundaries (start, after the neighbour search,
-// after the sorted gather, after the continuity pass, end).
+// ev (optional): 6 events recorded at stage boundaries (start, after the neighbour search,
+// after the sorted gather, after the neighbour lists, after the continuity pass, end).
 int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[0], s->stream));
   PG_TRY(enqueue_neighbors(s));
@@ -205,17 +205,18 @@ int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
   PG_TRY(launch_sph_gather(s->stream, a, s->arith));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[2], s->stream));
   PG_TRY(launch_sph_list(s->stream, a, s->arith, s->list_grid));
+  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
   if (rates) {
     PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_RATES, s->pass_grid[SPH_RATES]));
-    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
+    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
     s->launches += neighbor_launches(s) + 3;
   } else {
     PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_CONT, s->pass_grid[SPH_CONT]));
-    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
+    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
     PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM]));
     s->launches += neighbor_launches(s) + 4;
   }
-  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
+  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[5], s->stream));
   return PG_OK;
 }
 
@@ -253,14 +254,15 @@ int enqueue_dem_step(pg_system* s, cudaEvent_t* ev) {
   PG_TRY(launch_dem_gather(s->stream, a));
   PG_CUDA_TRY(cudaMemsetAsync(s->contacts.p, 0, sizeof(unsigned long long), s->stream));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[2], s->stream));
-  PG_TRY(launch_dem_pass(s->stream, a));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
+  PG_TRY(launch_dem_pass(s->stream, a));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
+  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[5], s->stream));
   s->launches += neighbor_launches(s) + 2;
   return PG_OK;
 }
 
-constexpr int kStepEvents = 5;
+constexpr int kStepEvents = 6;
 
 // Events for one timed step, from the pool.
 int timing_events(pg_system* s, cudaEvent_t** out) {
@@ -281,15 +283,17 @@ int timing_events(pg_system* s, cudaEvent_t** out) {
 int timing_collect(pg_system* s) {
   for (size_t b = 0; b + kStepEvents <= s->ev_pending.size(); b += kStepEvents) {
     cudaEvent_t* e = &s->ev_pending[b];
-    float t01, t12, t23, t24;
+    float t01, t12, t23, t34, t25;
     PG_CUDA_TRY(cudaEventElapsedTime(&t01, e[0], e[1]));
     PG_CUDA_TRY(cudaEventElapsedTime(&t12, e[1], e[2]));
     PG_CUDA_TRY(cudaEventElapsedTime(&t23, e[2], e[3]));
-    PG_CUDA_TRY(cudaEventElapsedTime(&t24, e[2], e[4]));
+    PG_CUDA_TRY(cudaEventElapsedTime(&t34, e[3], e[4]));
+    PG_CUDA_TRY(cudaEventElapsedTime(&t25, e[2], e[5]));
     s->tacc.neighbor_ms += t01;
     s->tacc.gather_ms += t12;
-    s->tacc.pass_ms += t24;
-    s->tacc.cont_ms += t23;
+    s->tacc.pass_ms += t25;
+    s->tacc.list_ms += t23;
+    s->tacc.cont_ms += t34;
     s->tacc.steps += 1;
   }
   // region: first start -> last end of the pending batch, added to the running region total
