@@ -25,11 +25,13 @@
 // with xE = x . E and P'(rho) = B ((gamma - 2)(rho/rho0)^gamma + 2) / rho^3 (all densities
 // are rho', the ones the momentum rate used).  Each thread evaluates Lam for all its
 // neighbours, so the transpose of the pair Jacobian is a second gather over the same cell
-// lists (no atomics, deterministic order).  The parameter derivatives take only the ordered
-// pair (i, j) of Phi_M:
-//   dPhi/dalpha += -m_j F (abar_i . x) (-2 c0 h) w / ((r^2 + eps h^2)(rho_i + rho_j))  (w < 0)
-//   dPhi/dB     += -m_j F (abar_i . x) (P_i + P_j) / B
-// accumulated per particle and summed in a fixed order at the end.
+// lists (no atomics, deterministic order).  The parameter derivatives are the derivatives of
+// Lam_M per unordered pair, each thread taking half of every pair it sees:
+//   dPhi/dalpha += -1/2 F xE (-2 c0 h) w / ((r^2 + eps h^2)(rho_i + rho_j))   (w < 0)
+//   dPhi/dB     += -1/2 F xE (P_i + P_j) / B
+// In this form the cancellation between the two ordered terms is done analytically inside E;
+// summing m_j F (abar_i . x_ij)(P_i + P_j) over j instead cancels across neighbours and loses
+// digits.  The per-particle sums are added in a fixed order at the end.
 //
 // Checkpointing: pg_forward_checkpointed keeps the state every `every` steps.  pg_backward
 // walks the segments last to first; for each it restores the checkpoint, re-runs the forward
@@ -61,6 +63,7 @@ struct pg_adjoint {
   pg::DevBuf lx, lv, lr, ga, gb;
   pg::DevBuf X4, V4, Q4, A4, PF, DB;  // slot-ordered packs of one adjoint step
   int pass_grid[3] = {0, 0, 0};
+  int pass_grid_fp32 = -1;
   size_t bytes() const {
     const pg::DevBuf* b[] = {&ckpt, &final_state, &seg_state, &seg_rnext, &seg_cell, &seg_id, &seg_start,
                              &lx,   &lv,          &lr,        &ga,        &gb,       &X4,     &V4,
@@ -208,12 +211,11 @@ struct AdjPairs {
     }
     const double PI = c1 * w;
     const double S = Pi + qj.x + PI;
-    double E[3], xE = 0.0, axd = 0.0;
+    double E[3], xE = 0.0;
 #pragma unroll
     for (int c = 0; c < DIM; ++c) {
       E[c] = mj * ai[c] - mi * (c == 0 ? aj.x : c == 1 ? aj.y : aj.z);
       xE += d[c] * E[c];
-      axd += ai[c] * d[c];
     }
     const double a1 = -G * S * xE + 2.0 * F * xE * PI / e;
     const double b1 = -F * c1 * xE;
@@ -224,9 +226,9 @@ struct AdjPairs {
       gv[c] += b1 * d[c];
     }
     gr -= F * xE * (Pdi - PI / rb);
-    const double own = mj * F * axd;
-    gal -= own * c1a * w;
-    gB -= own * (PBi + qj.z);
+    const double half = 0.5 * F * xE;
+    gal -= half * c1a * w;
+    gB -= half * (PBi + qj.z);
   }
 
   __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id, uint32_t k) {
@@ -259,37 +261,265 @@ struct AdjPairs {
   }
 };
 
+// ---------------------------------------------------------------------------------------
+// Mixed-precision adjoint (handles in the fast f64 mode).  Positions and velocities are packed
+// as FP32 (hi, lo) pairs, so the differences x_i - x_j and v_i - v_j keep FP32 relative
+// accuracy despite the cancellation; every other factor and the pair derivatives are FP32; the
+// adjoint state and the parameter sums stay double.
+//   s0 {x.hi, y.hi, z.hi, m} (also the prefilter positions)   s1 {x.lo, y.lo, z.lo, 0}
+//   s2 {vx.hi, vy.hi, vz.hi, rho'}   s3 {vx.lo, vy.lo, vz.lo, 0}   s4 {P, P', (P/B).hi, (P/B).lo}
+//   s5 {abar, 0}   s6 float dbar
+// dL/dB sums pair terms (P_i + P_j)/B whose signs follow compression and expansion, so P/B is
+// kept as (hi, lo) and the dL/dB terms are summed in double.
+// ---------------------------------------------------------------------------------------
+template <int DIM>
+__global__ void adjoint_prep_f_kernel(SphArgs a) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.n) return;
+  const uint32_t id = a.sorted_id[k];
+  const SphK& K = a.sys[0];
+  const double* pos = (const double*)a.pos;
+  const double* vel = (const double*)a.vel;
+  const double* lx = (const double*)a.lam[0];
+  const double* lv = (const double*)a.lam[1];
+  const double rho = ((const double*)a.rho)[id];
+  const double m = ((const double*)a.mass)[id];
+  const double dt = K.d.dt;
+  const bool fluid = id < K.fluid_end;
+  float hx[3] = {0.f, 0.f, 0.f}, lxs[3] = {0.f, 0.f, 0.f}, hv[3] = {0.f, 0.f, 0.f}, lvs[3] = {0.f, 0.f, 0.f};
+  float ab[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int c = 0; c < DIM; ++c) {
+    const size_t o = (size_t)id * DIM + c;
+    df_split(pos[o], &hx[c], &lxs[c]);
+    df_split(vel[o], &hv[c], &lvs[c]);
+    ab[c] = fluid ? (float)(dt * (lv[o] + dt * lx[o])) : 0.f;
+  }
+  const double rr = rho * K.d.inv_rho0;
+  double pw = rr;
+  for (int e = 1; e < K.gamma; ++e) pw *= rr;
+  const double inv_r2 = 1.0 / (rho * rho);
+  const double P = tait_pterm<OpsD>(K.d, K.gamma, rho);
+  const double Pd = K.d.B * ((double)(K.gamma - 2) * pw + 2.0) * inv_r2 / rho;
+  const double PB = (pw - 1.0) * inv_r2;
+  ((float4*)a.s[0])[k] = make_float4(hx[0], hx[1], hx[2], (float)m);
+  ((float4*)a.s[1])[k] = make_float4(lxs[0], lxs[1], lxs[2], 0.f);
+  ((float4*)a.s[2])[k] = make_float4(hv[0], hv[1], hv[2], (float)rho);
+  ((float4*)a.s[3])[k] = make_float4(lvs[0], lvs[1], lvs[2], 0.f);
+  float pbh, pbl;
+  df_split(PB, &pbh, &pbl);
+  ((float4*)a.s[4])[k] = make_float4((float)P, (float)Pd, pbh, pbl);
+  ((float4*)a.s[5])[k] = make_float4(ab[0], ab[1], ab[2], 0.f);
+}
+
+template <int DIM, int STAGE>
+struct AdjPairsF {
+  static constexpr bool kMom = STAGE == SPH_MOM;
+  const float4 *XH, *XL, *VH, *VL, *Q, *A;
+  const float* DBp;
+  float fa, fb, inv_h, four_h2, eps_h2, avk, avk_alpha;
+  float xh[3], xl[3], vh[3], vl[3], ai[3], rhoi, mi, Pi, Pdi, dbi;
+  double PBi;
+  float gx[3], gv[3], gr, gal;
+  float cx[3], cv[3], cr;  // compensation terms of gx, gv, gr (Kahan summation)
+  double gB;
+
+  __device__ __forceinline__ void begin(const SphArgs& a, const SphK& K, uint32_t k) {
+    XH = (const float4*)a.s[0];
+    XL = (const float4*)a.s[1];
+    VH = (const float4*)a.s[2];
+    VL = (const float4*)a.s[3];
+    Q = (const float4*)a.s[4];
+    A = (const float4*)a.s[5];
+    DBp = (const float*)a.s[6];
+    fa = (float)K.d.fa;
+    fb = (float)K.d.fb;
+    inv_h = (float)K.d.inv_h;
+    four_h2 = (float)K.d.four_h2;
+    eps_h2 = (float)K.d.eps_h2;
+    avk = (float)K.d.avk;
+    avk_alpha = (float)K.avk_alpha;
+    const float4 x = XH[k], x2 = XL[k], v = VH[k], v2 = VL[k];
+    xh[0] = x.x; xh[1] = x.y; xh[2] = x.z; mi = x.w;
+    xl[0] = x2.x; xl[1] = x2.y; xl[2] = x2.z;
+    vh[0] = v.x; vh[1] = v.y; vh[2] = v.z; rhoi = v.w;
+    vl[0] = v2.x; vl[1] = v2.y; vl[2] = v2.z;
+    Pi = Pdi = dbi = 0.f;
+    PBi = 0.0;
+    ai[0] = ai[1] = ai[2] = 0.f;
+    if (kMom) {
+      const float4 q = Q[k], ab = A[k];
+      Pi = q.x; Pdi = q.y; PBi = (double)q.z + (double)q.w;
+      ai[0] = ab.x; ai[1] = ab.y; ai[2] = ab.z;
+    } else {
+      dbi = DBp[k];
+    }
+    gx[0] = gx[1] = gx[2] = 0.f;
+    gv[0] = gv[1] = gv[2] = 0.f;
+    cx[0] = cx[1] = cx[2] = 0.f;
+    cv[0] = cv[1] = cv[2] = 0.f;
+    gr = gal = cr = 0.f;
+    gB = 0.0;
+  }
+
+  // s += y with the running compensation c (Kahan 1965); finish() adds s - c in double.
+  static __device__ __forceinline__ void kahan(float& s, float& c, float y) {
+    const float yc = __fsub_rn(y, c);
+    const float t = __fadd_rn(s, yc);
+    c = __fsub_rn(__fsub_rn(t, s), yc);
+    s = t;
+  }
+
+  __device__ __forceinline__ void pair(uint32_t t) {
+    const float4 xj = XH[t], xj2 = XL[t];
+    float d[3];
+    d[0] = (xh[0] - xj.x) + (xl[0] - xj2.x);
+    d[1] = (xh[1] - xj.y) + (xl[1] - xj2.y);
+    d[2] = DIM == 3 ? (xh[2] - xj.z) + (xl[2] - xj2.z) : 0.f;
+    float r2 = d[0] * d[0] + d[1] * d[1];
+    if (DIM == 3) r2 += d[2] * d[2];
+    // at r = 2h the spline's F and dF/dr vanish, so an FP32 cut-off there adds nothing
+    if (!(r2 < four_h2) || !(r2 > 0.f)) return;
+    const float4 vj = VH[t], vj2 = VL[t];
+    const float mj = xj.w;
+    float inv_r = rsqrtf(r2);
+    inv_r = inv_r * fmaf(-0.5f * r2 * inv_r, inv_r, 1.5f);  // one Newton step
+    const float r = r2 * inv_r;
+    const float q = r * inv_h;
+    float F, G;
+    if (q < 1.f) {
+      F = fa * (2.25f * q - 3.f);
+      G = fa * 2.25f * inv_h * inv_r;
+    } else {
+      const float tq = 2.f - q;
+      F = fb * tq * tq * inv_r;
+      G = -(fb * tq * inv_r) * (2.f * inv_h + tq * inv_r) * inv_r;
+    }
+    float dv[3];
+    dv[0] = (vh[0] - vj.x) + (vl[0] - vj2.x);
+    dv[1] = (vh[1] - vj.y) + (vl[1] - vj2.y);
+    dv[2] = DIM == 3 ? (vh[2] - vj.z) + (vl[2] - vj2.z) : 0.f;
+    float w = dv[0] * d[0] + dv[1] * d[1];
+    if (DIM == 3) w += dv[2] * d[2];
+    if (!kMom) {
+      const float D = dbi * mj + DBp[t] * mi;
+      const float gw = G * w * D, fd = F * D;
+#pragma unroll
+      for (int c = 0; c < DIM; ++c) {
+        kahan(gx[c], cx[c], gw * d[c] + fd * dv[c]);
+        kahan(gv[c], cv[c], fd * d[c]);
+      }
+      return;
+    }
+    const float4 qj = Q[t], aj = A[t];
+    const float rb = rhoi + vj.w;
+    const float e = r2 + eps_h2;
+    float c1 = 0.f, c1a = 0.f;
+    if (w < 0.f) {
+      const float base = 1.f / (e * rb);
+      c1 = avk * base;
+      c1a = avk_alpha * base;
+    }
+    const float PI = c1 * w;
+    const float S = Pi + qj.x + PI;
+    float E[3], xE = 0.f;
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+      E[c] = mj * ai[c] - mi * (c == 0 ? aj.x : c == 1 ? aj.y : aj.z);
+      xE += d[c] * E[c];
+    }
+    const float a1 = -G * S * xE + 2.f * F * xE * PI / e;
+    const float b1 = -F * c1 * xE;
+    const float fs = F * S;
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+      kahan(gx[c], cx[c], a1 * d[c] + b1 * dv[c] - fs * E[c]);
+      kahan(gv[c], cv[c], b1 * d[c]);
+    }
+    kahan(gr, cr, -F * xE * (Pdi - PI / rb));
+    const float half = 0.5f * F * xE;
+    gal -= half * c1a * w;
+    gB -= (double)half * (PBi + ((double)qj.z + (double)qj.w));
+  }
+
+  __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id, uint32_t k) {
+    double* lx = (double*)a.lam[0];
+    double* lv = (double*)a.lam[1];
+    double* lr = (double*)a.lam[2];
+    if (!kMom) {
+#pragma unroll
+      for (int c = 0; c < DIM; ++c) {
+        const size_t o = (size_t)id * DIM + c;
+        lx[o] += (double)gx[c] - (double)cx[c];
+        lv[o] += (double)gv[c] - (double)cv[c];
+      }
+      return;
+    }
+    const bool fluid = id < K.fluid_end;
+    const double dt = K.d.dt;
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+      const size_t o = (size_t)id * DIM + c;
+      const double lxo = lx[o];
+      lx[o] = lxo + ((double)gx[c] - (double)cx[c]);
+      lv[o] = (fluid ? lv[o] + dt * lxo : lv[o]) + ((double)gv[c] - (double)cv[c]);
+    }
+    const double lrt = lr[id] + ((double)gr - (double)cr);
+    lr[id] = lrt;
+    ((float*)a.s[6])[k] = (float)(dt * lrt);
+    ((double*)a.lam[3])[id] += (double)gal;
+    ((double*)a.lam[4])[id] += gB;
+  }
+};
+
 }  // namespace
 
-int launch_adjoint_prep(cudaStream_t st, const SphArgs& a) {
+int launch_adjoint_prep(cudaStream_t st, const SphArgs& a, bool fp32) {
   if (a.n == 0) return PG_OK;
   const unsigned b = (a.n + 255) / 256;
-  if (a.dim == 2) adjoint_prep_kernel<2><<<b, 256, 0, st>>>(a);
-  else adjoint_prep_kernel<3><<<b, 256, 0, st>>>(a);
+  if (fp32) {
+    if (a.dim == 2) adjoint_prep_f_kernel<2><<<b, 256, 0, st>>>(a);
+    else adjoint_prep_f_kernel<3><<<b, 256, 0, st>>>(a);
+  } else {
+    if (a.dim == 2) adjoint_prep_kernel<2><<<b, 256, 0, st>>>(a);
+    else adjoint_prep_kernel<3><<<b, 256, 0, st>>>(a);
+  }
   PG_CUDA_TRY(cudaGetLastError());
   return PG_OK;
 }
 
 typedef void (*AdjKernel)(SphArgs, int);
 
-AdjKernel adjoint_kernel(int dim, int stage) {
-  if (stage == SPH_MOM)
-    return dim == 2 ? sph_pass_kernel<AdjPairs<2, SPH_MOM>, 2, false> : sph_pass_kernel<AdjPairs<3, SPH_MOM>, 3, false>;
-  return dim == 2 ? sph_pass_kernel<AdjPairs<2, SPH_CONT>, 2, false> : sph_pass_kernel<AdjPairs<3, SPH_CONT>, 3, false>;
+template <int DIM>
+AdjKernel adjoint_kernel_dim(int stage, bool fp32) {
+  if (fp32)
+    return stage == SPH_MOM ? sph_list_pass_kernel<AdjPairsF<DIM, SPH_MOM>, DIM, false>
+                            : sph_list_pass_kernel<AdjPairsF<DIM, SPH_CONT>, DIM, false>;
+  return stage == SPH_MOM ? sph_list_pass_kernel<AdjPairs<DIM, SPH_MOM>, DIM, false>
+                          : sph_list_pass_kernel<AdjPairs<DIM, SPH_CONT>, DIM, false>;
 }
 
-int launch_adjoint_pass(cudaStream_t st, const SphArgs& a, int stage, int grid) {
+AdjKernel adjoint_kernel(int dim, int stage, bool fp32) {
+  return dim == 2 ? adjoint_kernel_dim<2>(stage, fp32) : adjoint_kernel_dim<3>(stage, fp32);
+}
+
+// Prefilter positions (float4 x, y, z) of the list kernel and of overflow walks: the FP64 packs
+// keep them in s4; the mixed-precision packs use the FP32 hi parts in s0.
+int adjoint_pf_index(bool fp32) { return fp32 ? 0 : 4; }
+
+int launch_adjoint_pass(cudaStream_t st, const SphArgs& a, int stage, int grid, bool fp32) {
   if (a.n == 0) return PG_OK;
   const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
   if (grid <= 0 || (uint32_t)grid > ntiles) grid = (int)ntiles;
-  adjoint_kernel(a.dim, stage)<<<grid, kSphThreads, 0, st>>>(a, 4);
+  adjoint_kernel(a.dim, stage, fp32)<<<grid, kSphThreads, 0, st>>>(a, adjoint_pf_index(fp32));
   PG_CUDA_TRY(cudaGetLastError());
   return PG_OK;
 }
 
-int adjoint_pass_occupancy(int dim, int stage) {
+int adjoint_pass_occupancy(int dim, int stage, bool fp32) {
   int blocks = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, adjoint_kernel(dim, stage), kSphThreads, 0);
+  cudaError_t e =
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, adjoint_kernel(dim, stage, fp32), kSphThreads, 0);
   return e == cudaSuccess ? blocks : 0;
 }
 
@@ -387,17 +617,21 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
   PG_TRY(A->lr.ensure(8 * nn));
   PG_TRY(A->ga.ensure(8 * nn));
   PG_TRY(A->gb.ensure(8 * nn));
+  // fast f64 handles: mixed-precision adjoint pair terms; IEEE handles: FP64
+  const bool fp32 = s->arith == pg::ARITH_F64_DF;
   PG_TRY(A->X4.ensure(32 * nn));
   PG_TRY(A->V4.ensure(32 * nn));
   PG_TRY(A->Q4.ensure(32 * nn));
   PG_TRY(A->A4.ensure(32 * nn));
   PG_TRY(A->PF.ensure(16 * nn));
   PG_TRY(A->DB.ensure(8 * nn));
-  if (A->pass_grid[pg::SPH_MOM] == 0) {
+  if (A->pass_grid_fp32 != (int)fp32 || A->pass_grid[pg::SPH_MOM] == 0) {
     int dev = 0, sms = 0;
     PG_CUDA_TRY(cudaGetDevice(&dev));
     PG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    for (int st = pg::SPH_CONT; st <= pg::SPH_MOM; ++st) A->pass_grid[st] = pg::adjoint_pass_occupancy(s->dim, st) * sms;
+    for (int st = pg::SPH_CONT; st <= pg::SPH_MOM; ++st)
+      A->pass_grid[st] = pg::adjoint_pass_occupancy(s->dim, st, fp32) * sms;
+    A->pass_grid_fp32 = (int)fp32;
   }
   if (nd) PG_CUDA_TRY(cudaMemcpyAsync(A->lx.p, dL_dx, 8 * nd, cudaMemcpyHostToDevice, s->stream));
   PG_CUDA_TRY(cudaMemsetAsync(A->lv.p, 0, 8 * nn * s->dim, s->stream));
@@ -406,12 +640,24 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
   PG_CUDA_TRY(cudaMemsetAsync(A->gb.p, 0, 8 * nn, s->stream));
 
   pg::SphArgs a = pg::sph_args(s, 0, false);
-  a.s[0] = A->X4.p;
-  a.s[1] = A->V4.p;
-  a.s[2] = A->Q4.p;
-  a.s[3] = A->A4.p;
-  a.s[4] = A->PF.p;
-  a.s[5] = A->DB.p;
+  if (fp32) {  // float4 packs, carved out of the FP64 pack buffers (same byte counts or less)
+    a.s[0] = A->X4.p;
+    a.s[1] = (char*)A->X4.p + 16 * nn;
+    a.s[2] = A->V4.p;
+    a.s[3] = (char*)A->V4.p + 16 * nn;
+    a.s[4] = A->Q4.p;
+    a.s[5] = A->A4.p;
+    a.s[6] = A->DB.p;
+    a.s[7] = nullptr;
+  } else {
+    a.s[0] = A->X4.p;
+    a.s[1] = A->V4.p;
+    a.s[2] = A->Q4.p;
+    a.s[3] = A->A4.p;
+    a.s[4] = A->PF.p;
+    a.s[5] = A->DB.p;
+    a.s[6] = a.s[7] = nullptr;
+  }
   a.lam[0] = A->lx.p;
   a.lam[1] = A->lv.p;
   a.lam[2] = A->lr.p;
@@ -445,9 +691,10 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
       a.sorted_cell = A->seg_cell.as<uint32_t>() + (size_t)t * n;
       a.sorted_id = A->seg_id.as<uint32_t>() + (size_t)t * n;
       a.cell_start = A->seg_start.as<uint32_t>() + (size_t)t * ncp1;
-      PG_TRY(pg::launch_adjoint_prep(s->stream, a));
-      PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_MOM, A->pass_grid[pg::SPH_MOM]));
-      PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_CONT, A->pass_grid[pg::SPH_CONT]));
+      PG_TRY(pg::launch_adjoint_prep(s->stream, a, fp32));
+      PG_TRY(pg::launch_sph_list_pf(s->stream, a, pg::adjoint_pf_index(fp32), s->list_grid));
+      PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_MOM, A->pass_grid[pg::SPH_MOM], fp32));
+      PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_CONT, A->pass_grid[pg::SPH_CONT], fp32));
     }
   }
   PG_TRY(pg::copy_state_in(s, A->final_state.as<double>()));

@@ -153,6 +153,7 @@ SphArgs sph_args(pg_system* s, int integrate, bool rates) {
   a.sorted_id = s->nw.sorted_id;
   a.cell_start = s->nw.cell_start.as<uint32_t>();
   for (int i = 0; i < 6; ++i) a.s[i] = s->sorted[i].p;
+  a.s[6] = a.s[7] = nullptr;
   a.pos = s->pos.p;
   a.vel = s->vel.p;
   a.rho = s->rho.p;

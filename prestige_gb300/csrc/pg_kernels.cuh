@@ -56,7 +56,7 @@ struct SphArgs {
   const uint32_t* sorted_cell;
   const uint32_t* sorted_id;
   const uint32_t* cell_start;
-  void* s[6];                // sorted packed arrays (layout per arithmetic mode)
+  void* s[8];                // sorted packed arrays (layout per arithmetic mode)
   void* pos;                 // canonical state, id order
   void* vel;
   void* rho;
@@ -79,12 +79,16 @@ int sph_pass_occupancy(int arith, int dim, int stage);
 int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid);
 int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid);
 int sph_list_occupancy(int arith, int dim, int stage);  // stage < 0: the list kernel
+// The list kernel with an explicit FP32 prefilter-position pack a.s[pf_index] (conservative test).
+int launch_sph_list_pf(cudaStream_t st, const SphArgs& a, int pf_index, int grid);
 
 // Adjoint of one SPH step (pg_adjoint.cu).  s[0..4] hold the slot-ordered packs written by
 // launch_adjoint_prep; pos/vel/rho/mass are the state before the step (id order).
-int launch_adjoint_prep(cudaStream_t st, const SphArgs& a);
-int launch_adjoint_pass(cudaStream_t st, const SphArgs& a, int stage, int grid);
-int adjoint_pass_occupancy(int dim, int stage);
+// fp32: mixed-precision packs and pair terms (double-precision adjoint accumulators).
+int launch_adjoint_prep(cudaStream_t st, const SphArgs& a, bool fp32);
+int launch_adjoint_pass(cudaStream_t st, const SphArgs& a, int stage, int grid, bool fp32);
+int adjoint_pass_occupancy(int dim, int stage, bool fp32);
+int adjoint_pf_index(bool fp32);
 // Bytes per particle of the sorted packed arrays s[0..5] for an arithmetic mode.
 void sph_sorted_layout(int arith, size_t sizes[6]);
 

@@ -506,6 +506,11 @@ int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid) {
   return launch_table(st, a, kern, pf, grid);
 }
 
+int launch_sph_list_pf(cudaStream_t st, const SphArgs& a, int pf_index, int grid) {
+  PassKernel kern = a.dim == 2 ? sph_list_kernel<2, false> : sph_list_kernel<3, false>;
+  return launch_table(st, a, kern, pf_index, grid);
+}
+
 int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid) {
   int pf = 0;
   PassKernel kern = list_kernel(arith, a.dim, stage, &pf);
