@@ -61,6 +61,7 @@ def parse():
     p.add_argument("--cpu-sample-n", type=int, default=0, help="particles in the CPU-baseline sample (0: auto)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the batched, adjoint and DEM sections")
+    p.add_argument("--no-autotune", action="store_true", help="keep the default block size and cell multiplier")
     return p.parse_args()
 
 
@@ -335,6 +336,9 @@ def run_gpu(args, rank, world, local, pgroup):
     n = w["n"]
     s = ParticleSystem(make_config(**w["config"]), n)
     workloads.load_into(s, w)
+    tuning = None
+    if not args.no_autotune:  # outside the timed region; the state is restored by the tuner
+        tuning = s.autotune(trial_steps=2)
     info = s.info()
 
     # ---- device-timed steps, state resident in HBM ----
@@ -426,7 +430,9 @@ def run_gpu(args, rank, world, local, pgroup):
             "gpu_launches": int(t["launches"]),
             "clocks": clk,
             "cpu_baseline": cpu,
-            "info": {"n_cells": info["n_cells"], "sort_passes": info["sort_passes"], "pass_grid": info["pass_grid"]},
+            "info": {"n_cells": info["n_cells"], "sort_passes": info["sort_passes"], "pass_grid": info["pass_grid"],
+                     "arith": info["arith"]},
+            "tuning": tuning,
         }
         if not args.no_extras:
             out["batched"] = bench_batched()

@@ -72,7 +72,7 @@ typedef struct pg_config {
   double wall_lo[3], wall_hi[3];
   int contact_capacity;
   /* tuning */
-  int block_size;     /* reserved (0) */
+  int block_size;     /* threads per block of the SPH list and pair kernels (0: 128; else a multiple of 32, <= 256) */
   int f64_mode;       /* pg_f64_mode */
   int list_capacity;  /* SPH neighbour-list slots per particle (0: 128 in 3D, 64 in 2D); a particle with
                          more neighbours is still handled exactly, by a slower continued walk */
@@ -196,11 +196,15 @@ int pg_dem_set_history(pg_system* sys, const uint32_t* partner, const double* xi
 int pg_forward_checkpointed(pg_system* sys, int nsteps, int every);
 int pg_backward(pg_system* sys, const double* dL_dx, double* dL_dalpha, double* dL_dB, double* dL_dv0);
 
-/* Autotuner: time candidate (cell multiplier, arithmetic mode) settings on the handle's current
- * state for `trial_steps` steps each, keep the fastest that meets the f64 tolerance, apply it and
- * report it.  The handle's state is restored afterwards. */
+/* Autotuner (SPH handles): time every (cell multiplier 1 or 1/2, arithmetic mode, block size 64,
+ * 128 or 256) on the handle's current state for `trial_steps` steps each, keep the fastest whose
+ * rates are within the mode's tolerance of the IEEE rates (1e-10 normwise for f64, 1e-4 for
+ * f32), apply it and report it.  The handle's state is restored afterwards; a graph-enabled handle
+ * is re-captured.  No reference counterpart (the reference has no executable backend to tune). */
 int pg_autotune(pg_system* sys, int trial_steps, int* best_block, double* best_multiplier, int* best_f64_mode,
                 double* best_ms_per_step);
+/* Apply a tuning found earlier (e.g. cached by the host) without searching. */
+int pg_set_tuning(pg_system* sys, int block, double cell_multiplier, int f64_mode);
 
 /* Device-side timing of steps (CUDA events on the handle's stream).  The momentum pass time is
  * pass_ms - list_ms - cont_ms.  pg_timing_enable(1) resets

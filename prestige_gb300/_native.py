@@ -85,6 +85,7 @@ SIGNATURES = {
     "pg_backward": (_I, [_P, _P, _P, _P, _P]),
     "pg_autotune": (_I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I),
                          ctypes.POINTER(ctypes.c_double)]),
+    "pg_set_tuning": (_I, [_P, _I, ctypes.c_double, _I]),
     "pg_timing_enable": (_I, [_P, _I]),
     "pg_timing_read": (_I, [_P, ctypes.POINTER(PgTiming)]),
     "pg_memory_bytes": (_I, [_P, ctypes.POINTER(_SZ)]),

@@ -692,7 +692,7 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
       a.sorted_id = A->seg_id.as<uint32_t>() + (size_t)t * n;
       a.cell_start = A->seg_start.as<uint32_t>() + (size_t)t * ncp1;
       PG_TRY(pg::launch_adjoint_prep(s->stream, a, fp32));
-      PG_TRY(pg::launch_sph_list_pf(s->stream, a, pg::adjoint_pf_index(fp32), s->list_grid));
+      PG_TRY(pg::launch_sph_list_pf(s->stream, a, pg::adjoint_pf_index(fp32), 0, pg::kSphThreads));
       PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_MOM, A->pass_grid[pg::SPH_MOM], fp32));
       PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_CONT, A->pass_grid[pg::SPH_CONT], fp32));
     }

@@ -205,16 +205,16 @@ int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
   SphArgs a = sph_args(s, integrate, rates);
   PG_TRY(launch_sph_gather(s->stream, a, s->arith));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[2], s->stream));
-  PG_TRY(launch_sph_list(s->stream, a, s->arith, s->list_grid));
+  PG_TRY(launch_sph_list(s->stream, a, s->arith, s->list_grid, s->block));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
   if (rates) {
-    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_RATES, s->pass_grid[SPH_RATES]));
+    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_RATES, s->pass_grid[SPH_RATES], s->block));
     if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
     s->launches += neighbor_launches(s) + 3;
   } else {
-    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_CONT, s->pass_grid[SPH_CONT]));
+    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_CONT, s->pass_grid[SPH_CONT], s->block));
     if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
-    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM]));
+    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], s->block));
     s->launches += neighbor_launches(s) + 4;
   }
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[5], s->stream));
@@ -395,19 +395,19 @@ int choose_pass_grid(pg_system* s) {
   PG_CUDA_TRY(cudaGetDevice(&dev));
   PG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   for (int st = 0; st < 3; ++st) {
-    const int occ = sph_list_occupancy(s->arith, s->dim, st);
+    const int occ = sph_list_occupancy(s->arith, s->dim, st, s->block);
     s->pass_grid[st] = occ > 0 ? occ * sms : 0;  // persistent: one resident wave
   }
-  const int locc = sph_list_occupancy(s->arith, s->dim, -1);
+  const int locc = sph_list_occupancy(s->arith, s->dim, -1, s->block);
   s->list_grid = locc > 0 ? locc * sms : 0;
   return PG_OK;
 }
 
-// Build grids, tables and buffers for the handle's configuration(s).
-int setup_system(pg_system* s) {
+// Cell grids of every system, their device copies and the neighbour-search workspace.
+int build_grids(pg_system* s, std::vector<GridK>& gk) {
   const int ns = s->nsys;
   s->grids.resize(ns);
-  std::vector<GridK> gk(ns);
+  gk.resize(ns);
   uint64_t cell_base = 0;
   for (int i = 0; i < ns; ++i) {
     const pg_config& c = s->cfgs[i];
@@ -429,6 +429,30 @@ int setup_system(pg_system* s) {
   PG_TRY(s->gridk.ensure(sizeof(GridK) * ns));
   PG_CUDA_TRY(cudaMemcpy(s->gridk.p, gk.data(), sizeof(GridK) * ns, cudaMemcpyHostToDevice));
   PG_TRY(s->nw.init(s->n, s->ncells));
+  return PG_OK;
+}
+
+// SPH per-system constants (device table).
+int build_sph_tables(pg_system* s, const std::vector<GridK>& gk) {
+  const int ns = s->nsys;
+  std::vector<SphK> k(ns);
+  for (int i = 0; i < ns; ++i) {
+    const pg_config& c = s->cfgs[i];
+    const size_t cnt = s->id_begin[i + 1] - s->id_begin[i];
+    const size_t nf = c.n_fluid < 0 || (size_t)c.n_fluid > cnt ? cnt : (size_t)c.n_fluid;
+    k[i] = make_sphk(c, s->grids[i], gk[i].cell_base, (uint32_t)s->id_begin[i], (uint32_t)s->id_begin[i + 1],
+                     (uint32_t)(s->id_begin[i] + nf));
+  }
+  PG_TRY(s->sphk.ensure(sizeof(SphK) * ns));
+  PG_CUDA_TRY(cudaMemcpy(s->sphk.p, k.data(), sizeof(SphK) * ns, cudaMemcpyHostToDevice));
+  return PG_OK;
+}
+
+// Build grids, tables and buffers for the handle's configuration(s).
+int setup_system(pg_system* s) {
+  const int ns = s->nsys;
+  std::vector<GridK> gk;
+  PG_TRY(build_grids(s, gk));
   if (ns > 1) {
     std::vector<uint32_t> soi(s->n);
     for (int i = 0; i < ns; ++i)
@@ -440,16 +464,7 @@ int setup_system(pg_system* s) {
   PG_TRY(s->err.ensure(sizeof(unsigned)));
   PG_CUDA_TRY(cudaMemset(s->err.p, 0, sizeof(unsigned)));
   if (s->model == PG_MODEL_SPH) {
-    std::vector<SphK> k(ns);
-    for (int i = 0; i < ns; ++i) {
-      const pg_config& c = s->cfgs[i];
-      const size_t cnt = s->id_begin[i + 1] - s->id_begin[i];
-      const size_t nf = c.n_fluid < 0 || (size_t)c.n_fluid > cnt ? cnt : (size_t)c.n_fluid;
-      k[i] = make_sphk(c, s->grids[i], gk[i].cell_base, (uint32_t)s->id_begin[i], (uint32_t)s->id_begin[i + 1],
-                       (uint32_t)(s->id_begin[i] + nf));
-    }
-    PG_TRY(s->sphk.ensure(sizeof(SphK) * ns));
-    PG_CUDA_TRY(cudaMemcpy(s->sphk.p, k.data(), sizeof(SphK) * ns, cudaMemcpyHostToDevice));
+    PG_TRY(build_sph_tables(s, gk));
     const size_t eb = pg_elem_bytes(s);
     PG_TRY(s->pos.ensure(eb * n * s->dim));
     PG_TRY(s->vel.ensure(eb * n * s->dim));
@@ -501,6 +516,38 @@ int setup_system(pg_system* s) {
     PG_TRY(s->contacts.ensure(sizeof(unsigned long long)));
     PG_CUDA_TRY(cudaMemset(s->contacts.p, 0, sizeof(unsigned long long)));
   }
+  return PG_OK;
+}
+
+// Re-derive grids, tables, sorted-pack layout and launch shapes of an SPH handle for a new cell
+// multiplier, arithmetic mode and block size.  The particle state is kept; graphs are dropped
+// (re-captured by the caller if it wants them).
+int retune_sph(pg_system* s, double mult, int f64_mode, int block) {
+  if (s->model != PG_MODEL_SPH) {
+    set_error("tuning applies to SPH handles");
+    return PG_EINVAL;
+  }
+  if (!(mult > 0.0) || (f64_mode != PG_F64_NATIVE && f64_mode != PG_F64_FAST) || block < 32 ||
+      block > kSphMaxThreads || block % 32) {
+    set_error("invalid tuning (multiplier %g, f64_mode %d, block %d)", mult, f64_mode, block);
+    return PG_EINVAL;
+  }
+  PG_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  drop_graphs(s);
+  for (auto& c : s->cfgs) {
+    c.cell_multiplier = mult;
+    c.f64_mode = f64_mode;
+    c.block_size = block;
+  }
+  s->cfg = s->cfgs[0];
+  std::vector<GridK> gk;
+  PG_TRY(build_grids(s, gk));
+  PG_TRY(build_sph_tables(s, gk));
+  s->arith = arith_of(s->cfg, s->f64);
+  s->block = block;
+  PG_TRY(ensure_sorted_buffers(s));
+  PG_TRY(choose_pass_grid(s));
+  s->nbr_valid = false;
   return PG_OK;
 }
 
@@ -628,6 +675,11 @@ static int create_common(const pg_config* cfgs, const size_t* counts, int nsys, 
     return PG_EINVAL;
   }
   s->list_cap = c0.list_capacity > 0 ? c0.list_capacity : (c0.dim == 2 ? 64 : 128);
+  if (c0.block_size != 0 && (c0.block_size < 32 || c0.block_size > kSphMaxThreads || c0.block_size % 32)) {
+    pg::set_error("block_size must be 0 or a multiple of 32 in 32..%d (got %d)", kSphMaxThreads, c0.block_size);
+    return PG_EINVAL;
+  }
+  s->block = c0.block_size > 0 ? c0.block_size : kSphThreads;
   s->n = total;
   s->nsys = nsys;
   s->id_begin.assign(nsys + 1, 0);

@@ -15,7 +15,8 @@ enum Arith {
   ARITH_F32_FAST = 3,   // single precision with fused multiply-add
 };
 
-constexpr int kSphThreads = 128;
+constexpr int kSphThreads = 128;     // block size of the two-phase pass and the default
+constexpr int kSphMaxThreads = 256;  // largest block size of the list-based kernels
 
 // Stages of the SPH pair pass.
 enum SphStage {
@@ -76,11 +77,12 @@ int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith);
 int launch_sph_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid);
 int sph_pass_occupancy(int arith, int dim, int stage);
 // Neighbour lists for the list-based passes (stage passes read a.nlist / a.nlen / a.nresume).
-int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid);
-int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid);
-int sph_list_occupancy(int arith, int dim, int stage);  // stage < 0: the list kernel
+// block: threads per block (multiple of 32, <= kSphMaxThreads).
+int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid, int block);
+int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid, int block);
+int sph_list_occupancy(int arith, int dim, int stage, int block);  // stage < 0: the list kernel
 // The list kernel with an explicit FP32 prefilter-position pack a.s[pf_index] (conservative test).
-int launch_sph_list_pf(cudaStream_t st, const SphArgs& a, int pf_index, int grid);
+int launch_sph_list_pf(cudaStream_t st, const SphArgs& a, int pf_index, int grid, int block);
 
 // Adjoint of one SPH step (pg_adjoint.cu).  s[0..4] hold the slot-ordered packs written by
 // launch_adjoint_prep; pos/vel/rho/mass are the state before the step (id order).

@@ -426,15 +426,19 @@ PassKernel list_kernel(int arith, int dim, int stage, int* pf_index) {
   return dim == 2 ? list_kernel_dim<2>(arith, stage, pf_index) : list_kernel_dim<3>(arith, stage, pf_index);
 }
 
-int launch_table(cudaStream_t st, const SphArgs& a, PassKernel kern, int pf, int grid) {
+int launch_table(cudaStream_t st, const SphArgs& a, PassKernel kern, int pf, int grid, int block) {
   if (!kern) {
     set_error("unknown arithmetic mode or stage");
     return PG_EINVAL;
   }
+  if (block < 32 || block > kSphMaxThreads || block % 32) {
+    set_error("block size %d must be a multiple of 32 in 32..%d", block, kSphMaxThreads);
+    return PG_EINVAL;
+  }
   if (a.n == 0) return PG_OK;
-  const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
+  const uint32_t ntiles = (a.n + block - 1) / block;
   if (grid <= 0 || (uint32_t)grid > ntiles) grid = (int)ntiles;
-  kern<<<grid, kSphThreads, 0, st>>>(a, pf);
+  kern<<<grid, block, 0, st>>>(a, pf);
   PG_CUDA_TRY(cudaGetLastError());
   return PG_OK;
 }
@@ -500,28 +504,28 @@ int launch_sph_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int
   return PG_OK;
 }
 
-int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid) {
+int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid, int block) {
   int pf = 0;
   PassKernel kern = list_kernel(arith, a.dim, -1, &pf);
-  return launch_table(st, a, kern, pf, grid);
+  return launch_table(st, a, kern, pf, grid, block);
 }
 
-int launch_sph_list_pf(cudaStream_t st, const SphArgs& a, int pf_index, int grid) {
+int launch_sph_list_pf(cudaStream_t st, const SphArgs& a, int pf_index, int grid, int block) {
   PassKernel kern = a.dim == 2 ? sph_list_kernel<2, false> : sph_list_kernel<3, false>;
-  return launch_table(st, a, kern, pf_index, grid);
+  return launch_table(st, a, kern, pf_index, grid, block);
 }
 
-int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid) {
+int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid, int block) {
   int pf = 0;
   PassKernel kern = list_kernel(arith, a.dim, stage, &pf);
-  return launch_table(st, a, kern, pf, grid);
+  return launch_table(st, a, kern, pf, grid, block);
 }
 
-int sph_list_occupancy(int arith, int dim, int stage) {
+int sph_list_occupancy(int arith, int dim, int stage, int block) {
   int pf = 0, blocks = 0;
   PassKernel kern = list_kernel(arith, dim, stage, &pf);
   if (!kern) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, kSphThreads, 0) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, block, 0) != cudaSuccess) return 0;
   return blocks;
 }
 

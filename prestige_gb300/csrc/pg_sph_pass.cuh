@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kSphThreads) sph_pass_kernel(SphArgs a, int pf
 // did not fit, so the pair passes can continue the walk from there.
 // ---------------------------------------------------------------------------------------
 template <int DIM, bool EXACT_PF>
-__global__ void __launch_bounds__(kSphThreads) sph_list_kernel(SphArgs a, int pf_index) {
+__global__ void __launch_bounds__(kSphMaxThreads) sph_list_kernel(SphArgs a, int pf_index) {
   const int tid = threadIdx.x;
   const float4* __restrict__ PF = (const float4*)a.s[pf_index];
   const uint32_t* __restrict__ start = a.cell_start;
@@ -178,11 +178,12 @@ __global__ void __launch_bounds__(kSphThreads) sph_list_kernel(SphArgs a, int pf
   const int side = 2 * R + 1;
   const int nrows = side * (2 * RZ + 1);
   const uint32_t cap = a.cap;
-  const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
+  const uint32_t bs = blockDim.x;
+  const uint32_t ntiles = (a.n + bs - 1) / bs;
 
   for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const SphK* Kp;
-    const Target T = target_of(a, tile * kSphThreads + tid, &Kp, R);
+    const Target T = target_of(a, tile * bs + tid, &Kp, R);
     const SphK& K = *Kp;
     const GridK& g = K.g;
     const float4 pi = PF[T.k];
@@ -219,15 +220,17 @@ __global__ void __launch_bounds__(kSphThreads) sph_list_kernel(SphArgs a, int pf
   }
 }
 
-// Pair pass over the lists of sph_list_kernel.  Lanes step through their lists together;
+// Pair pass over the lists of sph_list_kernel (any block size up to kSphMaxThreads, a
+// multiple of 32).  Lanes step through their lists together;
 // a list that overflowed is followed by the rest of the walk from its resume point.
 template <class Pairs, int DIM, bool EXACT_PF>
-__global__ void __launch_bounds__(kSphThreads) sph_list_pass_kernel(SphArgs a, int pf_index) {
+__global__ void __launch_bounds__(kSphMaxThreads) sph_list_pass_kernel(SphArgs a, int pf_index) {
   const int tid = threadIdx.x;
   const uint32_t cap = a.cap;
-  const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
+  const uint32_t bs = blockDim.x;
+  const uint32_t ntiles = (a.n + bs - 1) / bs;
   for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const uint32_t k0 = tile * kSphThreads + tid;
+    const uint32_t k0 = tile * bs + tid;
     const bool live = k0 < a.n;
     const uint32_t k = live ? k0 : a.n - 1;
     const uint32_t id = a.sorted_id[k];

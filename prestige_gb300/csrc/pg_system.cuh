@@ -48,6 +48,7 @@ struct pg_system {
   pg::DevBuf tmp, tmp2, tmp3, tmp4;
   int pass_grid[3] = {0, 0, 0};  // per SphStage
   int list_grid = 0;
+  int block = 128;               // threads per block of the list-based SPH kernels
   int list_cap = 128;            // neighbour-list slots per particle
   pg::DevBuf nlist, nlen, nresume;
 
@@ -86,6 +87,8 @@ int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev);
 long long neighbor_launches(const pg_system* s);
 int sync_and_check(pg_system* s);
 int choose_pass_grid(pg_system* s);
+int retune_sph(pg_system* s, double mult, int f64_mode, int block);
+int enqueue_step(pg_system* s);
 void drop_graphs(pg_system* s);
 int capture_graphs(pg_system* s);
 void destroy_adjoint(pg_system* s);

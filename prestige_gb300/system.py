@@ -6,6 +6,8 @@ prestige/src/equations/ir.rs:3-14) -- and runs the fused pair loop on the GPU in
 generated CPU text loop (prestige/src/codegen/simple_cpu.rs:3-22).
 """
 import ctypes
+import json
+import os
 
 import numpy as np
 
@@ -219,15 +221,45 @@ class ParticleSystem:
         return da.value, dB.value, dv0.reshape(self.n, self.dim)
 
     # -- tuning and introspection ---------------------------------------------------------------------
-    def autotune(self, trial_steps=3):
+    def tuning_key(self):
+        """Cache key of a tuning: dimension, precision and particle-count bucket (powers of 2)."""
+        bucket = 1 << max(self.n - 1, 0).bit_length()
+        return "dim%d-%s-n%d" % (self.dim, "f64" if self.f64 else "f32", bucket)
+
+    def autotune(self, trial_steps=3, cache=None):
+        """Run pg_autotune, or apply the cached result for this handle's key when `cache` (a JSON
+        file path) holds one.  A new result is written to the cache."""
+        key = self.tuning_key()
+        if cache is not None and os.path.exists(cache):
+            with open(cache) as f:
+                table = json.load(f)
+            if key in table:
+                t = table[key]
+                self.set_tuning(t["block_size"], t["cell_multiplier"], t["f64_mode"])
+                return dict(t, cached=True)
         blk = ctypes.c_int()
         mult = ctypes.c_double()
         mode = ctypes.c_int()
         ms = ctypes.c_double()
         nat.check(self._lib.pg_autotune(self._h, int(trial_steps), ctypes.byref(blk), ctypes.byref(mult),
                                         ctypes.byref(mode), ctypes.byref(ms)), "pg_autotune")
-        return {"block_size": blk.value, "cell_multiplier": mult.value, "f64_mode": mode.value,
-                "ms_per_step": ms.value}
+        res = {"block_size": blk.value, "cell_multiplier": mult.value, "f64_mode": mode.value,
+               "ms_per_step": ms.value}
+        if cache is not None:
+            table = {}
+            if os.path.exists(cache):
+                with open(cache) as f:
+                    table = json.load(f)
+            table[key] = res
+            tmp = cache + ".tmp"
+            with open(tmp, "w") as f:
+                json.dump(table, f, indent=1, sort_keys=True)
+            os.replace(tmp, cache)
+        return dict(res, cached=False)
+
+    def set_tuning(self, block_size, cell_multiplier, f64_mode):
+        nat.check(self._lib.pg_set_tuning(self._h, int(block_size), float(cell_multiplier), int(f64_mode)),
+                  "pg_set_tuning")
 
     def info(self):
         i = nat.PgInfo()
