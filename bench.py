@@ -54,7 +54,8 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--n", type=int, default=4096000)
+    # (--particles, not --n: torch.distributed.run would read --n as an abbreviation of its own options)
+    p.add_argument("--particles", "--n", dest="n", type=int, default=4096000)
     p.add_argument("--precision", default="f64", choices=["f64", "f32"])
     p.add_argument("--mode", default="fast", choices=["fast", "native"])
     p.add_argument("--e2e-steps", type=int, default=5)

@@ -50,6 +50,12 @@ def load():
     return _lib
 
 
+def _p(a):
+    """Host pointer of a numpy array as a ctypes void pointer (a bare Python
+    int would be passed as a C int)."""
+    return ctypes.c_void_p(a.ctypes.data)
+
+
 def num_threads(n=0):
     return load().orc_num_threads(int(n))
 
@@ -57,7 +63,7 @@ def num_threads(n=0):
 def _cols(pos, dtype):
     pos = np.asarray(pos)
     dim = pos.shape[1]
-    cols = [np.ascontiguousarray(pos[:, d], dtype=dtype) for d in range(dim)]
+    cols = [np.array(pos[:, d], dtype=dtype, copy=True) for d in range(dim)]
     if dim == 2:
         cols.append(np.zeros(pos.shape[0], dtype=dtype))
     return cols
@@ -88,9 +94,9 @@ def cell_list(pos, lo, hi, support, mult=1.0, f64=True):
     cell = np.empty(n, np.uint32)
     sid = np.empty(n, np.uint32)
     start = np.empty(g["ncells"] + 1, np.uint32)
-    load().orc_cell_list(dim, 1 if f64 else 0, ctypes.c_longlong(n), cols[0].ctypes.data, cols[1].ctypes.data,
-                         cols[2].ctypes.data, _d(lo), _d(hi), ctypes.c_double(support), ctypes.c_double(mult),
-                         cell.ctypes.data, sid.ctypes.data, start.ctypes.data)
+    load().orc_cell_list(dim, 1 if f64 else 0, ctypes.c_longlong(n), _p(cols[0]), _p(cols[1]),
+                         _p(cols[2]), _d(lo), _d(hi), ctypes.c_double(support), ctypes.c_double(mult),
+                         _p(cell), _p(sid), _p(start))
     return cell, sid, start
 
 
@@ -99,9 +105,9 @@ def neighbor_counts(pos, lo, hi, support, mult=1.0, f64=True):
     n, dim = np.asarray(pos).shape
     cols = _cols(pos, dt)
     out = np.empty(n, np.uint32)
-    load().orc_neighbor_counts(dim, 1 if f64 else 0, ctypes.c_longlong(n), cols[0].ctypes.data, cols[1].ctypes.data,
-                               cols[2].ctypes.data, _d(lo), _d(hi), ctypes.c_double(support), ctypes.c_double(mult),
-                               out.ctypes.data)
+    load().orc_neighbor_counts(dim, 1 if f64 else 0, ctypes.c_longlong(n), _p(cols[0]), _p(cols[1]),
+                               _p(cols[2]), _d(lo), _d(hi), ctypes.c_double(support), ctypes.c_double(mult),
+                               _p(out))
     return out
 
 
@@ -113,9 +119,9 @@ def neighbor_list(pos, lo, hi, support, mult=1.0, f64=True):
     cap = int(counts.sum())
     offs = np.empty(n + 1, np.uint64)
     nbr = np.empty(max(cap, 1), np.uint32)
-    st = load().orc_neighbor_list(dim, 1 if f64 else 0, ctypes.c_longlong(n), cols[0].ctypes.data,
-                                  cols[1].ctypes.data, cols[2].ctypes.data, _d(lo), _d(hi), ctypes.c_double(support),
-                                  ctypes.c_double(mult), offs.ctypes.data, nbr.ctypes.data, ctypes.c_uint64(cap))
+    st = load().orc_neighbor_list(dim, 1 if f64 else 0, ctypes.c_longlong(n), _p(cols[0]),
+                                  _p(cols[1]), _p(cols[2]), _d(lo), _d(hi), ctypes.c_double(support),
+                                  ctypes.c_double(mult), _p(offs), _p(nbr), ctypes.c_uint64(cap))
     assert st == 0
     return offs, nbr[:cap]
 
@@ -126,9 +132,9 @@ def gather_sum(pos, lo, hi, support, src, dst, mult=1.0, f64=True):
     cols = _cols(pos, dt)
     src = np.ascontiguousarray(src, np.float64)
     out = np.array(dst, dtype=np.float64, copy=True)
-    load().orc_gather_sum(dim, 1 if f64 else 0, ctypes.c_longlong(n), cols[0].ctypes.data, cols[1].ctypes.data,
-                          cols[2].ctypes.data, _d(lo), _d(hi), ctypes.c_double(support), ctypes.c_double(mult),
-                          src.ctypes.data, out.ctypes.data)
+    load().orc_gather_sum(dim, 1 if f64 else 0, ctypes.c_longlong(n), _p(cols[0]), _p(cols[1]),
+                          _p(cols[2]), _d(lo), _d(hi), ctypes.c_double(support), ctypes.c_double(mult),
+                          _p(src), _p(out))
     return out
 
 
@@ -160,7 +166,8 @@ class SphState:
         dt = np.float64 if f64 else np.float32
         self.f64 = f64
         self.n, self.dim = np.asarray(pos).shape
-        self.cols = _cols(pos, dt) + _cols(vel, dt) + [np.ascontiguousarray(rho, dt), np.ascontiguousarray(mass, dt)]
+        # always copies: the oracle advances these columns in place
+        self.cols = _cols(pos, dt) + _cols(vel, dt) + [np.array(rho, dt, copy=True), np.array(mass, dt, copy=True)]
 
     def ptrs(self):
         return (ctypes.c_void_p * 8)(*[c.ctypes.data for c in self.cols])
@@ -205,7 +212,7 @@ def sph_grad_dual(cfg, state, u, target, nsteps):
     tptr = (ctypes.c_void_p * 3)(*[c.ctypes.data for c in tcols])
     out = np.zeros(4)
     load().orc_sph_grad_dual(ctypes.byref(spec), ctypes.c_longlong(state.n), state.ptrs(), uptr, tptr, int(nsteps),
-                             out.ctypes.data)
+                             _p(out))
     return out
 
 
@@ -228,8 +235,9 @@ class DemState:
         n = np.asarray(pos).shape[0]
         self.n = n
         self.capacity = capacity
+        # always copies: the oracle advances these columns in place
         self.cols = (_cols(pos, np.float64) + _cols(vel, np.float64) + _cols(omega, np.float64)
-                     + [np.ascontiguousarray(radius, np.float64), np.ascontiguousarray(mass, np.float64)])
+                     + [np.array(radius, np.float64, copy=True), np.array(mass, np.float64, copy=True)])
         self.hpid = np.full(n * capacity, 0xFFFFFFFF, np.uint32)
         self.hxi = np.zeros(n * capacity * 3, np.float64)
 
@@ -253,6 +261,6 @@ def dem_run(cfg, state, nsteps):
     """Advance in place; returns (contacts of the last step or -1 on slot overflow, seconds)."""
     spec = dem_spec(cfg)
     sec = ctypes.c_double()
-    c = load().orc_dem_run(ctypes.byref(spec), ctypes.c_longlong(state.n), state.ptrs(), state.hpid.ctypes.data,
-                           state.hxi.ctypes.data, int(nsteps), ctypes.byref(sec))
+    c = load().orc_dem_run(ctypes.byref(spec), ctypes.c_longlong(state.n), state.ptrs(), _p(state.hpid),
+                           _p(state.hxi), int(nsteps), ctypes.byref(sec))
     return c, sec.value

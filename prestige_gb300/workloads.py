@@ -171,6 +171,28 @@ def dem_settling(n=200000, box=(0.1, 0.1, 0.3), seed=1, capacity=16, cell_multip
             "fields": {"pos": x, "vel": np.zeros_like(x), "omega": np.zeros_like(x), "radius": r, "mass": m}}
 
 
+def dem_compressed_lattice(nside=(8, 8, 8), r=0.5e-3, overlap=0.02, seed=0, capacity=16):
+    """Spheres on a cubic lattice spaced 2r(1 - overlap) with small jitter, random velocities and
+    spins, inside walls that touch the outer layer: every contact path (normal, tangential
+    history, Coulomb slip, torques, walls) is active from the first step."""
+    rng = np.random.default_rng(seed)
+    nside = tuple(nside) if hasattr(nside, "__len__") else (nside,) * 3
+    sp = 2 * r * (1 - overlap)
+    idx = np.stack(np.meshgrid(*[np.arange(k) for k in nside], indexing="ij"), -1).reshape(-1, 3)
+    pos = (idx + 0.5) * sp + rng.uniform(-0.05, 0.05, size=idx.shape) * r
+    n = pos.shape[0]
+    radius = r * (1 + rng.uniform(-0.05, 0.0, size=n))
+    mass = 2600 * 4 / 3 * np.pi * radius ** 3
+    vel = rng.normal(0, 0.05, size=(n, 3))
+    omega = rng.normal(0, 50.0, size=(n, 3))
+    box = np.array(nside) * sp
+    cfg = dict(model=1, dim=3, precision=1, domain_lo=[-2e-3] * 3, domain_hi=list(box + 2e-3), cell_multiplier=1.0,
+               gravity=[0, 0, -9.81], dt=1e-6, kn=1e5, restitution=0.9, mu=0.3, kt=1e5 * 2 / 7, r_max=r,
+               wall_lo=[0, 0, 0], wall_hi=list(box - 0.01 * r), contact_capacity=capacity)
+    return {"config": cfg, "n": n, "fields": {"pos": pos, "vel": vel, "omega": omega, "radius": radius,
+                                              "mass": mass}}
+
+
 # ------------------------------------------------------------------------------------------
 # Batched dam breaks
 # ------------------------------------------------------------------------------------------
