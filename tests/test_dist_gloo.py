@@ -23,8 +23,9 @@ def _free_port():
 
 
 def _worker(rank, world, port, out_dir):
+    # CPU ranks over gloo, also on a machine with GPUs
     os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank), MASTER_ADDR="127.0.0.1",
-                      MASTER_PORT=str(port))
+                      MASTER_PORT=str(port), CUDA_VISIBLE_DEVICES="")
     sys.path.insert(0, ROOT)
     import bench
     r, w, _, pg = bench.dist_setup()
@@ -55,7 +56,7 @@ def test_reference_arm_under_torchrun_prints_one_line_from_rank0():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
            "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"), "--impl", "reference",
            "--gpus", "2", "--particles", "4096", "--steps", "2", "--warmup", "1"]
-    env = dict(os.environ, OMP_NUM_THREADS="2")
+    env = dict(os.environ, OMP_NUM_THREADS="2", CUDA_VISIBLE_DEVICES="")
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, env=env, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
