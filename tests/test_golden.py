@@ -1,16 +1,16 @@
 """Committed golden fixtures (tests/golden/oracle_small.npz, made by tests/golden/make_golden.py).
 
-CPU: the oracle reproduces every fixture bit for bit (guards the oracle against drift across
-builds and hosts).  GPU: the CUDA path reproduces the fixtures: cell lists, neighbour counts and
-IEEE SPH results bit for bit, the double-word mode within 1e-10, DEM within 1e-13 (its damping
-coefficient goes through the host libm's log, which may differ by an ulp between hosts).
+CPU: the oracle reproduces every fixture from the stored inputs, bit for bit (DEM within 1e-13),
+which guards it against drift across builds and hosts.  GPU: the CUDA path reproduces the
+fixtures: cell lists, neighbour counts and IEEE SPH results bit for bit, the double-word mode
+within 1e-10, DEM within 1e-13 (its damping coefficient goes through the host libm's log, which
+may differ by an ulp between hosts).
 """
+import json
 import os
 
 import numpy as np
 import pytest
-
-from prestige_gb300 import workloads
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "oracle_small.npz")
 
@@ -20,19 +20,31 @@ def golden():
     return np.load(GOLDEN)
 
 
-@pytest.fixture(scope="module")
-def regenerated(oracle):
+def _mod():
     import importlib.util
     spec = importlib.util.spec_from_file_location("make_golden", os.path.join(os.path.dirname(GOLDEN), "make_golden.py"))
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
-    return mod.cases()
+    return mod
 
 
-def test_oracle_reproduces_golden(golden, regenerated):
-    assert set(golden.files) == set(regenerated)
-    for k in golden.files:
-        assert np.array_equal(golden[k], regenerated[k]), k
+def _case(golden, name):
+    """Workload dict of a stored case: its configuration and input arrays."""
+    cfg = json.loads(str(golden["configs"]))[name]
+    pre = name + "_in_"
+    fields = {k[len(pre):]: golden[k] for k in golden.files if k.startswith(pre)}
+    return {"config": cfg, "n": fields["pos"].shape[0], "fields": fields}
+
+
+def test_oracle_reproduces_golden(golden, oracle):
+    cfgs = json.loads(str(golden["configs"]))
+    arrays = {k: golden[k] for k in golden.files if "_in_" in k}
+    res = _mod().results(cfgs, arrays)
+    for k in res:
+        if k.startswith("dem_") and k != "dem_contacts10":  # libm log in the damping coefficient
+            assert np.abs(golden[k] - res[k]).max() <= 1e-13 * np.abs(golden[k]).max(), k
+        else:
+            assert np.array_equal(golden[k], res[k]), k
 
 
 def _sph(w, precision=1, mode=0):
@@ -47,7 +59,7 @@ def _sph(w, precision=1, mode=0):
 
 @pytest.mark.gpu
 def test_gpu_cell_list_and_counts_match_golden(pg, golden):
-    s = _sph(workloads.sph_lattice_3d(n=1000, seed=2))
+    s = _sph(_case(golden, "lattice"))
     cell, ids, start = s.neighbors()
     assert np.array_equal(ids, golden["lattice_sorted_id"])
     assert np.array_equal(cell, golden["lattice_cell"][golden["lattice_sorted_id"]])
@@ -57,7 +69,7 @@ def test_gpu_cell_list_and_counts_match_golden(pg, golden):
 
 @pytest.mark.gpu
 def test_gpu_sph_matches_golden(pg, golden):
-    w = workloads.sph_lattice_3d(n=1000, seed=2)
+    w = _case(golden, "lattice")
     s = _sph(w)
     acc, drho = s.compute_rates()
     assert np.array_equal(acc, golden["lattice_acc"]) and np.array_equal(drho, golden["lattice_drho"])
@@ -73,16 +85,15 @@ def test_gpu_sph_matches_golden(pg, golden):
     fast.step(5)
     ref = golden["lattice_pos5"]
     assert np.abs(fast.get("pos") - ref).max() <= 1e-10 * np.abs(ref).max()
-    wd = workloads.dam_break_2d(dx=0.1)
-    d = _sph(wd)
+    d = _sph(_case(golden, "dam"))
     d.step(5)
     assert np.array_equal(d.get("pos"), golden["dam_pos5"]) and np.array_equal(d.get("rho"), golden["dam_rho5"])
 
 
 @pytest.mark.gpu
 def test_gpu_dem_matches_golden(pg, golden):
-    from prestige_gb300 import ParticleSystem
-    w = workloads.dem_compressed_lattice(nside=4)
+    from prestige_gb300 import ParticleSystem, workloads
+    w = _case(golden, "dem")
     s = ParticleSystem(w["config"], w["n"])
     workloads.load_into(s, w)
     s.step(10)
