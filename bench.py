@@ -63,6 +63,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the batched, adjoint and DEM sections")
     p.add_argument("--no-autotune", action="store_true", help="keep the default block size and cell multiplier")
+    p.add_argument("--section", default="all", choices=["all", "batched", "adjoint", "dem"],
+                   help="run only one extra section and print its JSON (for profiling)")
     return p.parse_args()
 
 
@@ -333,6 +335,11 @@ def run_gpu(args, rank, world, local, pgroup):
     from prestige_gb300 import ParticleSystem, make_config, workloads
 
     torch.cuda.set_device(local)
+    if args.section != "all":
+        if rank == 0:
+            fn = {"batched": bench_batched, "adjoint": bench_adjoint, "dem": bench_dem}[args.section]
+            print(json.dumps({"section": args.section, args.section: fn()}), flush=True)
+        return
     w = workload(args)
     n = w["n"]
     s = ParticleSystem(make_config(**w["config"]), n)

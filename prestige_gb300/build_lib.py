@@ -15,6 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libprestige_gpu.so")
+HOST_DIR = os.path.join(HERE, "host")
+HOST_LIB = os.path.join(OUT_DIR, "libprestige_host.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -60,8 +62,29 @@ def _compile(src, verbose):
     return obj
 
 
+def build_host(force=False):
+    """The C++ host layer (prestige_gb300/host): libprestige_host.so, linked to the CUDA library."""
+    srcs = [os.path.join(HOST_DIR, f) for f in os.listdir(HOST_DIR) if f.endswith((".cpp", ".hpp"))]
+    if not force and not _stale(HOST_LIB, srcs + [LIB, __file__, os.path.join(INCLUDE, "prestige_gpu.h")]):
+        return HOST_LIB
+    tmp = HOST_LIB + ".tmp%d" % os.getpid()
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", "-o", tmp,
+           os.path.join(HOST_DIR, "prestige_host.cpp"), "-L", OUT_DIR, "-lprestige_gpu", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("host layer build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, HOST_LIB)
+    return HOST_LIB
+
+
 def build(force=False, verbose=False):
-    """Compile the library if any source is newer than it; return the .so path."""
+    """Compile the library (and the C++ host layer) if any source is newer; return the .so path."""
+    lib = _build_cuda(force, verbose)
+    build_host(force)
+    return lib
+
+
+def _build_cuda(force=False, verbose=False):
     os.makedirs(OUT_DIR, exist_ok=True)
     srcs = sources()
     if not force and not _stale(LIB, srcs + headers() + [__file__]):
