@@ -65,6 +65,9 @@ def parse():
     p.add_argument("--no-autotune", action="store_true", help="keep the default block size and cell multiplier")
     p.add_argument("--section", default="all", choices=["all", "batched", "adjoint", "dem"],
                    help="run only one extra section and print its JSON (for profiling)")
+    p.add_argument("--adjoint-steps", type=int, default=500)
+    p.add_argument("--adjoint-every", type=int, default=50)
+    p.add_argument("--adjoint-modes", default="native,fast", help="comma list of native, fast")
     return p.parse_args()
 
 
@@ -278,7 +281,7 @@ def bench_batched(steps=20, looped_steps=5, sync_steps=2):
             "timing": "host wall clock around graph-replayed steps, stream synchronised"}
 
 
-def bench_adjoint(nsteps=500, every=50, n=100000):
+def bench_adjoint(nsteps=500, every=50, n=100000, modes=("native", "fast")):
     """Differentiable 3D SPH: forward with checkpoints, then the adjoint sweep (recompute +
     adjoint passes); cost of a backward step over a forward step."""
     import torch
@@ -288,6 +291,8 @@ def bench_adjoint(nsteps=500, every=50, n=100000):
     out = {"workload": "100,000-particle jittered lattice, 8 Fourier velocity modes (0.05 m/s), loss = mean "
                        "squared distance to a seeded target, %d steps, checkpoints every %d" % (nsteps, every)}
     for mode, name in ((0, "native"), (1, "fast")):
+        if name not in modes:
+            continue
         s = ParticleSystem(make_config(**dict(w["config"], f64_mode=mode)), n)
         workloads.load_into(s, w)
         s.step(3)
@@ -337,8 +342,11 @@ def run_gpu(args, rank, world, local, pgroup):
     torch.cuda.set_device(local)
     if args.section != "all":
         if rank == 0:
-            fn = {"batched": bench_batched, "adjoint": bench_adjoint, "dem": bench_dem}[args.section]
-            print(json.dumps({"section": args.section, args.section: fn()}), flush=True)
+            if args.section == "adjoint":
+                res = bench_adjoint(args.adjoint_steps, args.adjoint_every, modes=args.adjoint_modes.split(","))
+            else:
+                res = {"batched": bench_batched, "dem": bench_dem}[args.section]()
+            print(json.dumps({"section": args.section, args.section: res}), flush=True)
         return
     w = workload(args)
     n = w["n"]
@@ -444,7 +452,8 @@ def run_gpu(args, rank, world, local, pgroup):
         }
         if not args.no_extras:
             out["batched"] = bench_batched()
-            out["adjoint"] = bench_adjoint()
+            out["adjoint"] = bench_adjoint(args.adjoint_steps, args.adjoint_every,
+                                           modes=args.adjoint_modes.split(","))
             out["dem"] = bench_dem()
         print(json.dumps(out), flush=True)
 

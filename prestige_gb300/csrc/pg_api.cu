@@ -165,6 +165,7 @@ SphArgs sph_args(pg_system* s, int integrate, bool rates) {
   a.nlen = s->nlen.as<uint32_t>();
   a.nresume = s->nresume.as<uint32_t>();
   a.cap = (uint32_t)s->list_cap;
+  a.err = s->err.as<unsigned>();
   return a;
 }
 
@@ -233,6 +234,7 @@ DemArgs dem_args(pg_system* s) {
   a.sA = s->sorted[0].as<double4_32a>();
   a.sB = s->sorted[1].as<double4_32a>();
   a.sW = s->sorted[2].as<double4_32a>();
+  a.sF = s->sorted[3].as<float4>();
   a.pos = s->pos.as<double>();
   a.vel = s->vel.as<double>();
   a.omega = s->omega.as<double>();
@@ -506,6 +508,7 @@ int setup_system(pg_system* s) {
     PG_CUDA_TRY(cudaMemset(s->radius.p, 0, 8 * n));
     PG_CUDA_TRY(cudaMemset(s->mass.p, 0, 8 * n));
     for (int i = 0; i < 3; ++i) PG_TRY(s->sorted[i].ensure(32 * n));
+    PG_TRY(s->sorted[3].ensure(16 * n));
     const size_t C = (size_t)c.contact_capacity;
     for (int b = 0; b < 2; ++b) {
       PG_TRY(s->hpid[b].ensure(4 * n * C));

@@ -70,6 +70,7 @@ struct SphArgs {
   uint32_t* nlen;            // neighbours of slot k that passed the prefilter (may exceed cap)
   uint32_t* nresume;         // (row, slot) where the walk continues when nlen[k] > cap
   uint32_t cap;
+  unsigned* err;             // device error word (ERR_* bits)
   int integrate;
 };
 
@@ -134,6 +135,7 @@ struct DemArgs {
   double4_32a* sA;  // x, y, z, r
   double4_32a* sB;  // vx, vy, vz, m
   double4_32a* sW;  // wx, wy, wz, 0
+  float4* sF;       // x, y, z, r rounded to FP32 (conservative candidate prefilter)
   double* pos;
   double* vel;
   double* omega;

@@ -181,3 +181,17 @@ def test_list_overflow_continues_the_walk(pg, oracle, cap, precision, mode):
     else:
         assert _rel(acc, oacc) <= F64_TOL and _rel(drho, odrho) <= F64_TOL
         assert _rel(s.get("pos"), st.pos) <= F64_TOL
+
+
+@pytest.mark.parametrize("mult", [0.4, 0.5, 1.0])
+def test_steps_bit_exact_across_cell_sizes(pg, oracle, mult):
+    """Neighbour rows staged in shared memory (reach 1 and 2) and the global walk (reach 3)
+    give the oracle's results for the same cell multiplier."""
+    w = workloads.sph_lattice_3d(n=4000, seed=41, cell_multiplier=mult)
+    s, cfg = _pair(w, 1, 0)
+    st = _ostate(oracle, w)
+    s.step(2)
+    oracle.sph_run(cfg, st, 2)
+    assert np.array_equal(s.get("pos"), st.pos)
+    assert np.array_equal(s.get("rho"), st.rho)
+    assert s.info()["reach"] == (3 if mult == 0.4 else 2 if mult == 0.5 else 1)
