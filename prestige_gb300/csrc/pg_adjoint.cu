@@ -267,10 +267,9 @@ struct AdjPairs {
 // accuracy despite the cancellation; every other factor and the pair derivatives are FP32; the
 // adjoint state and the parameter sums stay double.
 //   s0 {x.hi, y.hi, z.hi, m} (also the prefilter positions)   s1 {x.lo, y.lo, z.lo, 0}
-//   s2 {vx.hi, vy.hi, vz.hi, rho'}   s3 {vx.lo, vy.lo, vz.lo, 0}   s4 {P, P', (P/B).hi, (P/B).lo}
+//   s2 {vx.hi, vy.hi, vz.hi, rho'}   s3 {vx.lo, vy.lo, vz.lo, 0}   s4 {P, P', P/B, 0}
 //   s5 {abar, 0}   s6 float dbar
-// dL/dB sums pair terms (P_i + P_j)/B whose signs follow compression and expansion, so P/B is
-// kept as (hi, lo) and the dL/dB terms are summed in double.
+// Per-particle sums (adjoint increments and parameter terms) use Kahan compensation.
 // ---------------------------------------------------------------------------------------
 template <int DIM>
 __global__ void adjoint_prep_f_kernel(SphArgs a) {
@@ -306,9 +305,7 @@ __global__ void adjoint_prep_f_kernel(SphArgs a) {
   ((float4*)a.s[1])[k] = make_float4(lxs[0], lxs[1], lxs[2], 0.f);
   ((float4*)a.s[2])[k] = make_float4(hv[0], hv[1], hv[2], (float)rho);
   ((float4*)a.s[3])[k] = make_float4(lvs[0], lvs[1], lvs[2], 0.f);
-  float pbh, pbl;
-  df_split(PB, &pbh, &pbl);
-  ((float4*)a.s[4])[k] = make_float4((float)P, (float)Pd, pbh, pbl);
+  ((float4*)a.s[4])[k] = make_float4((float)P, (float)Pd, (float)PB, 0.f);
   ((float4*)a.s[5])[k] = make_float4(ab[0], ab[1], ab[2], 0.f);
 }
 
@@ -318,11 +315,9 @@ struct AdjPairsF {
   const float4 *XH, *XL, *VH, *VL, *Q, *A;
   const float* DBp;
   float fa, fb, inv_h, four_h2, eps_h2, avk, avk_alpha;
-  float xh[3], xl[3], vh[3], vl[3], ai[3], rhoi, mi, Pi, Pdi, dbi;
-  double PBi;
-  float gx[3], gv[3], gr, gal;
-  float cx[3], cv[3], cr;  // compensation terms of gx, gv, gr (Kahan summation)
-  double gB;
+  float xh[3], xl[3], vh[3], vl[3], ai[3], rhoi, mi, Pi, Pdi, PBi, dbi;
+  float gx[3], gv[3], gr, gal, gB;
+  float cx[3], cv[3], cr, ca, cb;  // compensation terms (Kahan summation)
 
   __device__ __forceinline__ void begin(const SphArgs& a, const SphK& K, uint32_t k) {
     XH = (const float4*)a.s[0];
@@ -344,12 +339,11 @@ struct AdjPairsF {
     xl[0] = x2.x; xl[1] = x2.y; xl[2] = x2.z;
     vh[0] = v.x; vh[1] = v.y; vh[2] = v.z; rhoi = v.w;
     vl[0] = v2.x; vl[1] = v2.y; vl[2] = v2.z;
-    Pi = Pdi = dbi = 0.f;
-    PBi = 0.0;
+    Pi = Pdi = PBi = dbi = 0.f;
     ai[0] = ai[1] = ai[2] = 0.f;
     if (kMom) {
       const float4 q = Q[k], ab = A[k];
-      Pi = q.x; Pdi = q.y; PBi = (double)q.z + (double)q.w;
+      Pi = q.x; Pdi = q.y; PBi = q.z;
       ai[0] = ab.x; ai[1] = ab.y; ai[2] = ab.z;
     } else {
       dbi = DBp[k];
@@ -358,8 +352,7 @@ struct AdjPairsF {
     gv[0] = gv[1] = gv[2] = 0.f;
     cx[0] = cx[1] = cx[2] = 0.f;
     cv[0] = cv[1] = cv[2] = 0.f;
-    gr = gal = cr = 0.f;
-    gB = 0.0;
+    gr = gal = gB = cr = ca = cb = 0.f;
   }
 
   // s += y with the running compensation c (Kahan 1965); finish() adds s - c in double.
@@ -438,8 +431,8 @@ struct AdjPairsF {
     }
     kahan(gr, cr, -F * xE * (Pdi - PI / rb));
     const float half = 0.5f * F * xE;
-    gal -= half * c1a * w;
-    gB -= (double)half * (PBi + ((double)qj.z + (double)qj.w));
+    kahan(gal, ca, -half * c1a * w);
+    kahan(gB, cb, -half * (PBi + qj.z));
   }
 
   __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id, uint32_t k) {
@@ -467,8 +460,8 @@ struct AdjPairsF {
     const double lrt = lr[id] + ((double)gr - (double)cr);
     lr[id] = lrt;
     ((float*)a.s[6])[k] = (float)(dt * lrt);
-    ((double*)a.lam[3])[id] += (double)gal;
-    ((double*)a.lam[4])[id] += gB;
+    ((double*)a.lam[3])[id] += (double)gal - (double)ca;
+    ((double*)a.lam[4])[id] += (double)gB - (double)cb;
   }
 };
 
