@@ -229,7 +229,7 @@ struct DfPairs {
   double four_h2;
   double xid[3];
   df xi[3], vi[3], rhoi, Pi;
-  df acc[3], dr;
+  dfacc acc[3], dr;
 
   __device__ __forceinline__ void begin(const SphArgs& a, const SphK& K, uint32_t k) {
     Ah = (const float4*)a.s[0];
@@ -251,8 +251,8 @@ struct DfPairs {
     }
     const double4_32a xd = Xd[k];
     xid[0] = xd.x; xid[1] = xd.y; xid[2] = xd.z;
-    acc[0] = acc[1] = acc[2] = df_make(0.f, 0.f);
-    dr = df_make(0.f, 0.f);
+    acc[0] = acc[1] = acc[2] = dfacc_zero();
+    dr = dfacc_zero();
   }
 
   // The oracle's f64 neighbour test, used only when the double-word r^2 is within a relative
@@ -273,8 +273,7 @@ struct DfPairs {
     const df d0 = df_sub(xi[0], df_make(ah.x, al.x));
     const df d1 = df_sub(xi[1], df_make(ah.y, al.y));
     const df d2 = DIM == 3 ? df_sub(xi[2], df_make(ah.z, al.z)) : df_make(0.f, 0.f);
-    df r2 = df_add(df_mul(d0, d0), df_mul(d1, d1));
-    if (DIM == 3) r2 = df_add(r2, df_mul(d2, d2));
+    const df r2 = df_sumsq3(d0, d1, d2);
     const df gap = df_sub(r2, df_make(w.four_h2[0], w.four_h2[1]));
     if (fabsf(gap.hi) <= w.band) {
       if (!exact_test(t)) return;
@@ -295,10 +294,10 @@ struct DfPairs {
     const float4 bh = Bh[t], bl = Bl[t];
     const df dv0 = df_sub(vi[0], df_make(bh.x, bl.x));
     const df dv1 = df_sub(vi[1], df_make(bh.y, bl.y));
-    df wv = df_add(df_mul(dv0, d0), df_mul(dv1, d1));
-    if (DIM == 3) wv = df_add(wv, df_mul(df_sub(vi[2], df_make(bh.z, bl.z)), d2));
+    const df dv2 = DIM == 3 ? df_sub(vi[2], df_make(bh.z, bl.z)) : df_make(0.f, 0.f);
+    const df wv = df_dot3(dv0, dv1, dv2, d0, d1, d2);
     const df mj = df_make(ah.w, al.w);
-    if (kCont) dr = df_add(dr, df_mul(mj, df_mul(wv, F)));
+    if (kCont) dfacc_add_prod(dr, mj, df_mul(wv, F));
     if (kMom) {
       const float4 rpj = RP[t];
       df pij = df_make(0.f, 0.f);
@@ -306,10 +305,10 @@ struct DfPairs {
         const df den = df_mul(df_add(r2, df_make(w.eps_h2[0], w.eps_h2[1])), df_add(rhoi, df_make(rpj.x, rpj.y)));
         pij = df_div(df_mul(df_make(w.avk[0], w.avk[1]), wv), den);
       }
-      const df coef = df_mul(mj, df_mul(df_add(df_add(Pi, df_make(rpj.z, rpj.w)), pij), F));
-      acc[0] = df_sub(acc[0], df_mul(coef, d0));
-      acc[1] = df_sub(acc[1], df_mul(coef, d1));
-      if (DIM == 3) acc[2] = df_sub(acc[2], df_mul(coef, d2));
+      const df ncoef = df_neg(df_mul(mj, df_mul(df_add(df_add(Pi, df_make(rpj.z, rpj.w)), pij), F)));
+      dfacc_add_prod(acc[0], ncoef, d0);
+      dfacc_add_prod(acc[1], ncoef, d1);
+      if (DIM == 3) dfacc_add_prod(acc[2], ncoef, d2);
     }
   }
 
@@ -317,11 +316,11 @@ struct DfPairs {
     const SphC<double>& c = K.d;
     if (STAGE == SPH_RATES) {
 #pragma unroll
-      for (int cc = 0; cc < DIM; ++cc) ((double*)a.acc)[(size_t)id * DIM + cc] = df_to_double(acc[cc]);
-      ((double*)a.drho)[id] = df_to_double(dr);
+      for (int cc = 0; cc < DIM; ++cc) ((double*)a.acc)[(size_t)id * DIM + cc] = dfacc_to_double(acc[cc]);
+      ((double*)a.drho)[id] = dfacc_to_double(dr);
     } else if (STAGE == SPH_CONT) {
       double* rho = (double*)a.rho;
-      const double rn = __dadd_rn(rho[id], __dmul_rn(c.dt, df_to_double(dr)));
+      const double rn = __dadd_rn(rho[id], __dmul_rn(c.dt, dfacc_to_double(dr)));
       rho[id] = rn;
       ((float4*)a.s[4])[k] = df_pack_rho_p(rn, tait_pterm<OpsD>(c, K.gamma, rn));
     } else if (id < K.fluid_end) {
@@ -330,7 +329,7 @@ struct DfPairs {
 #pragma unroll
       for (int cc = 0; cc < DIM; ++cc) {
         const size_t o = (size_t)id * DIM + cc;
-        const double v = __dadd_rn(vel[o], __dmul_rn(c.dt, __dadd_rn(df_to_double(acc[cc]), c.g[cc])));
+        const double v = __dadd_rn(vel[o], __dmul_rn(c.dt, __dadd_rn(dfacc_to_double(acc[cc]), c.g[cc])));
         vel[o] = v;
         pos[o] = __dadd_rn(pos[o], __dmul_rn(c.dt, v));
       }
