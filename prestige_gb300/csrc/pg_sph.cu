@@ -268,23 +268,24 @@ struct DfPairs {
     return r2 < four_h2 && r2 > 0.0;
   }
 
-  __device__ __forceinline__ void pair(uint32_t t) {
+  // Geometry of pair (k, t): x_ij, r^2, F = (dW/dr)/r and w = v_ij . x_ij.  False when t is not
+  // a neighbour (outside the support, or t == k).
+  __device__ __forceinline__ bool geometry(uint32_t t, df* d, df& r2, df& F, df& wv, df& mj) const {
     const float4 ah = Ah[t], al = Al[t];
-    const df d0 = df_sub(xi[0], df_make(ah.x, al.x));
-    const df d1 = df_sub(xi[1], df_make(ah.y, al.y));
-    const df d2 = DIM == 3 ? df_sub(xi[2], df_make(ah.z, al.z)) : df_make(0.f, 0.f);
-    const df r2 = df_sumsq3(d0, d1, d2);
+    d[0] = df_sub(xi[0], df_make(ah.x, al.x));
+    d[1] = df_sub(xi[1], df_make(ah.y, al.y));
+    d[2] = DIM == 3 ? df_sub(xi[2], df_make(ah.z, al.z)) : df_make(0.f, 0.f);
+    r2 = df_sumsq3(d[0], d[1], d[2]);
     const df gap = df_sub(r2, df_make(w.four_h2[0], w.four_h2[1]));
     if (fabsf(gap.hi) <= w.band) {
-      if (!exact_test(t)) return;
+      if (!exact_test(t)) return false;
     } else if (!(gap.hi < 0.f)) {
-      return;
+      return false;
     }
-    if (!(r2.hi > 0.f)) return;
+    if (!(r2.hi > 0.f)) return false;
     const df inv_r = df_rsqrt(r2);
     const df r = df_mul(r2, inv_r);
     const df q = df_mul(r, df_make(w.inv_h[0], w.inv_h[1]));
-    df F;
     if (q.hi < 1.0f) {
       F = df_mul(df_make(w.fa[0], w.fa[1]), df_add_f(df_mul_f(q, 2.25f), -3.0f));
     } else {
@@ -295,21 +296,29 @@ struct DfPairs {
     const df dv0 = df_sub(vi[0], df_make(bh.x, bl.x));
     const df dv1 = df_sub(vi[1], df_make(bh.y, bl.y));
     const df dv2 = DIM == 3 ? df_sub(vi[2], df_make(bh.z, bl.z)) : df_make(0.f, 0.f);
-    const df wv = df_dot3(dv0, dv1, dv2, d0, d1, d2);
-    const df mj = df_make(ah.w, al.w);
-    if (kCont) dfacc_add_prod(dr, mj, df_mul(wv, F));
-    if (kMom) {
-      const float4 rpj = RP[t];
-      df pij = df_make(0.f, 0.f);
-      if (wv.hi < 0.f) {
-        const df den = df_mul(df_add(r2, df_make(w.eps_h2[0], w.eps_h2[1])), df_add(rhoi, df_make(rpj.x, rpj.y)));
-        pij = df_div(df_mul(df_make(w.avk[0], w.avk[1]), wv), den);
-      }
-      const df ncoef = df_neg(df_mul(mj, df_mul(df_add(df_add(Pi, df_make(rpj.z, rpj.w)), pij), F)));
-      dfacc_add_prod(acc[0], ncoef, d0);
-      dfacc_add_prod(acc[1], ncoef, d1);
-      if (DIM == 3) dfacc_add_prod(acc[2], ncoef, d2);
+    wv = df_dot3(dv0, dv1, dv2, d[0], d[1], d[2]);
+    mj = df_make(ah.w, al.w);
+    return true;
+  }
+
+  __device__ __forceinline__ void momentum(uint32_t t, const df* d, df r2, df F, df wv, df mj) {
+    const float4 rpj = RP[t];
+    df pij = df_make(0.f, 0.f);
+    if (wv.hi < 0.f) {
+      const df den = df_mul(df_add(r2, df_make(w.eps_h2[0], w.eps_h2[1])), df_add(rhoi, df_make(rpj.x, rpj.y)));
+      pij = df_div(df_mul(df_make(w.avk[0], w.avk[1]), wv), den);
     }
+    const df ncoef = df_neg(df_mul(mj, df_mul(df_add(df_add(Pi, df_make(rpj.z, rpj.w)), pij), F)));
+    dfacc_add_prod(acc[0], ncoef, d[0]);
+    dfacc_add_prod(acc[1], ncoef, d[1]);
+    if (DIM == 3) dfacc_add_prod(acc[2], ncoef, d[2]);
+  }
+
+  __device__ __forceinline__ void pair(uint32_t t) {
+    df d[3], r2, F, wv, mj;
+    if (!geometry(t, d, r2, F, wv, mj)) return;
+    if (kCont) dfacc_add_prod(dr, mj, df_mul(wv, F));
+    if (kMom) momentum(t, d, r2, F, wv, mj);
   }
 
   __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id, uint32_t k) {
