@@ -165,6 +165,23 @@ int pg_cell_list_noalloc(const double* pos, size_t n, int dim, const double doma
  * (j == i included).  dst and src name scalar double slices. */
 int pg_gather_sum(pg_system* sys, const char* dst, const char* src);
 
+/* GPU execution of pairwise equations given as source text: the GPU counterpart of the
+ * reference's generate_simple_cpu (prestige/src/codegen/simple_cpu.rs:3-22), which only
+ * returns the text of `for i in 0..n { for j in 0..n { bodies } }`.  Here the fused bodies run
+ * for every particle i and every neighbour j with |x_i - x_j| < support (j == i included), in
+ * the traversal order of pg_gather_sum.  Body syntax: `x[i] op= expr` (op: = += -= *= /=) and
+ * `let name = expr` statements over slices x[i] / x[j] (user double fields; "mass" and "rho"
+ * read-only in double-precision SPH systems), the pair geometry dx dy dz r2 r, `support`, and
+ * sqrt exp ln abs min max powi powf sin cos (as calls or Rust methods).  Reads of x[j] see the
+ * values before the call.  The kernel is compiled with NVRTC at first use for the device and
+ * cached by its source; PG_ESTATE if NVRTC is not available, PG_EINVAL (message in
+ * pg_last_error) for a body outside the grammar.  IEEE double without contraction:
+ * {"force[i] += mass[j]"} reproduces pg_gather_sum bit for bit. */
+int pg_run_equations(pg_system* sys, const char* const* bodies, int n_bodies);
+/* The CUDA source pg_run_equations would compile for `bodies` (every slice taken as a double
+ * field), for inspection and tests; *needed receives the size including the terminating zero. */
+int pg_equation_source(const char* const* bodies, int n_bodies, char* out, size_t capacity, size_t* needed);
+
 /* SPH: evaluate the fused continuity + momentum rates without integrating ("acc" without
  * gravity, "drho").  The GPU form of one generate_simple_cpu loop over the fused SPH equations
  * (prestige/src/equations/fuse.rs:14-40, prestige/src/codegen/simple_cpu.rs:3-22). */

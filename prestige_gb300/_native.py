@@ -74,6 +74,8 @@ SIGNATURES = {
     "pg_get_neighbor_list": (_I, [_P, _P, _P, _SZ, ctypes.POINTER(_SZ)]),
     "pg_gather_sum": (_I, [_P, _S, _S]),
     "pg_compute_rates": (_I, [_P]),
+    "pg_run_equations": (_I, [_P, ctypes.POINTER(_S), _I]),
+    "pg_equation_source": (_I, [ctypes.POINTER(_S), _I, _P, _SZ, ctypes.POINTER(_SZ)]),
     "pg_step": (_I, [_P, _I]),
     "pg_step_async": (_I, [_P, _I]),
     "pg_sync": (_I, [_P]),

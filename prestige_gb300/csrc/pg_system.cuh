@@ -39,6 +39,7 @@ struct pg_system {
   pg::DevBuf omega, radius;        // DEM
   pg::DevBuf acc, drho;            // rates output (pg_compute_rates)
   std::map<std::string, std::unique_ptr<pg::DevBuf>> user;  // user scalar fields (double)
+  std::map<std::string, std::unique_ptr<pg::DevBuf>> snapshots;  // pre-call copies (pg_run_equations)
 
   // neighbour search and sorted copies
   pg::NbrWork nw;

@@ -13,8 +13,8 @@ Reference (dineshadepu/prestige):
 Differences, all deliberate: reads/writes are listed in first-appearance order (the reference
 collects them through a HashSet, so its order is unspecified); the body is the function's source
 text.  `run_gpu` executes a fused set on the GPU with j restricted to the neighbour set
-{j : |x_i - x_j| < support}; bodies it does not recognise raise instead of falling back to a
-CPU loop.
+{j : |x_i - x_j| < support} (a compiled kernel for general bodies); bodies outside the equation
+grammar raise instead of falling back to a CPU loop.
 """
 import ast
 import inspect
@@ -164,19 +164,35 @@ def _gather_pattern(body):
     return (t.value.id, v.value.id) if ok else None
 
 
+def check_bodies(bodies):
+    """Validate bodies with the library's equation translator (no device needed); raises
+    ValueError with its message for a body outside the grammar."""
+    import ctypes
+
+    from . import _native
+    lib = _native.load()
+    arr = (ctypes.c_char_p * len(bodies))(*[b.encode() for b in bodies])
+    need = ctypes.c_size_t()
+    if lib.pg_equation_source(arr, len(bodies), None, 0, ctypes.byref(need)) != _native.PG_OK:
+        raise ValueError(lib.pg_last_error().decode())
+
+
 def run_gpu(fused, system):
     """Execute a fused equation set on the GPU handle `system` (a ParticleSystem).
 
-    Recognised bodies: `dst[i] += src[j]` (the reference's eq1 form) -> pg_gather_sum; the
-    built-in SPH continuity + momentum pair -> pg_compute_rates.  Anything else raises."""
+    The built-in SPH continuity + momentum pair -> pg_compute_rates; a single `dst[i] += src[j]`
+    (the reference's eq1 form) -> pg_gather_sum; any other set -> one kernel compiled from the
+    bodies (pg_run_equations).  Bodies outside the equation grammar raise ValueError; there is
+    no CPU fallback."""
     names = set(fused.bodies)
-    if names and names <= {SPH_CONTINUITY.body, SPH_MOMENTUM.body}:
+    if not names:
+        raise ValueError("empty equation set")
+    if names <= {SPH_CONTINUITY.body, SPH_MOMENTUM.body}:
         return system.compute_rates()
-    for b in fused.bodies:
-        pat = _gather_pattern(b)
-        if pat is None:
-            raise NotImplementedError("no GPU kernel for equation body: %r" % b)
-    for b in fused.bodies:
-        dst, src = _gather_pattern(b)
+    if len(fused.bodies) == 1 and _gather_pattern(fused.bodies[0]) is not None:
+        dst, src = _gather_pattern(fused.bodies[0])
         system.gather_sum(dst, src)
+        return None
+    check_bodies(fused.bodies)
+    system.run_equations(list(fused.bodies))
     return None

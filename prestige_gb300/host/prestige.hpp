@@ -8,8 +8,10 @@
 //   generate_simple_cpu   prestige/src/codegen/simple_cpu.rs:3-22  the all-pairs loop text
 //   debug_equation        prestige/src/equations/debug.rs:3-22
 // and adds the GPU backend the reference does not have: run_gpu() executes a fused set on a
-// System (a device-resident particle handle) with j restricted to the neighbour set.  Bodies
-// it does not recognise raise; there is no CPU fallback.
+// System (a device-resident particle handle) with j restricted to the neighbour set: the
+// built-in SPH pair through the SPH pass, a single `dst[i] += src[j]` through the gather kernel,
+// anything else as one kernel compiled from the bodies (pg_run_equations).  Bodies outside the
+// equation grammar raise; there is no CPU fallback.
 //
 // Differences from the reference, all deliberate: equation() takes the body as text (C++ has
 // no procedural macros); reads and writes keep first-appearance order (the reference collects
@@ -85,6 +87,7 @@ class System {
   void step(int nsteps = 1);
   void compute_rates();
   void gather_sum(const std::string& dst, const std::string& src);
+  void run_equations(const std::vector<std::string>& bodies);
 
   struct Gradients {
     double dL_dalpha = 0.0;
@@ -103,16 +106,17 @@ class System {
   int model_ = PG_MODEL_SPH;
 };
 
-// What run_gpu will do for a fused set, validated without touching a device: one action per
-// body.  Throws std::invalid_argument for a body with no GPU kernel.
+// What run_gpu will do for a fused set, validated without touching a device.  Throws
+// std::invalid_argument (with the translator's message) for a body outside the grammar.
 struct GpuAction {
-  enum Kind { GatherSum, SphRates } kind;
+  enum Kind { GatherSum, SphRates, Compiled } kind;
   std::string dst, src;  // GatherSum: dst[i] += src[j]
 };
 std::vector<GpuAction> plan_gpu(const FusedEquations& fused);
 
-// Executes a fused set on the GPU: `dst[i] += src[j]` (the reference's eq1 form,
-// prestige/src/lib.rs:10) through pg_gather_sum; the built-in SPH pair through pg_compute_rates.
+// Executes a fused set on the GPU: the built-in SPH pair through pg_compute_rates; a single
+// `dst[i] += src[j]` (the reference's eq1 form, prestige/src/lib.rs:10) through pg_gather_sum;
+// any other set as one compiled kernel (pg_run_equations).
 void run_gpu(const FusedEquations& fused, System& sys);
 
 }  // namespace prestige

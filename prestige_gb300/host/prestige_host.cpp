@@ -225,6 +225,12 @@ void System::gather_sum(const std::string& dst, const std::string& src) {
   check(pg_gather_sum(h_, dst.c_str(), src.c_str()), "pg_gather_sum");
 }
 
+void System::run_equations(const std::vector<std::string>& bodies) {
+  std::vector<const char*> b;
+  for (const std::string& x : bodies) b.push_back(x.c_str());
+  check(pg_run_equations(h_, b.data(), (int)b.size()), "pg_run_equations");
+}
+
 void System::forward_checkpointed(int nsteps, int every) {
   check(pg_forward_checkpointed(h_, nsteps, every), "pg_forward_checkpointed");
 }
@@ -241,32 +247,37 @@ System::Gradients System::backward(const std::vector<double>& dL_dx) {
 // GPU backend
 // ---------------------------------------------------------------------------------------
 std::vector<GpuAction> plan_gpu(const FusedEquations& fused) {
+  if (fused.bodies.empty()) throw std::invalid_argument("empty equation set");
   const std::string cont = strip(sph_continuity().body), mom = strip(sph_momentum().body);
-  bool all_sph = !fused.bodies.empty();
+  bool all_sph = true;
   for (const std::string& b : fused.bodies) {
     const std::string s = strip(b);
     all_sph = all_sph && (s == cont || s == mom);
   }
   if (all_sph) return {GpuAction{GpuAction::SphRates, "", ""}};
-  std::vector<GpuAction> plan;
-  for (const std::string& b : fused.bodies) {
-    // exactly `dst[i] += src[j]`
-    const std::vector<Token> t = tokenize(b);
+  if (fused.bodies.size() == 1) {  // exactly `dst[i] += src[j]`
+    const std::vector<Token> t = tokenize(fused.bodies[0]);
     size_t m = t.size();
     while (m > 0 && t[m - 1].text == ";") --m;
     const bool ok = m == 9 && t[0].kind == Token::Ident && t[1].text == "[" && t[2].text == "i" && t[3].text == "]" &&
                     t[4].text == "+=" && t[5].kind == Token::Ident && t[6].text == "[" && t[7].text == "j" &&
                     t[8].text == "]";
-    if (!ok) throw std::invalid_argument("no GPU kernel for equation body: " + b);
-    plan.push_back(GpuAction{GpuAction::GatherSum, t[0].text, t[5].text});
+    if (ok) return {GpuAction{GpuAction::GatherSum, t[0].text, t[5].text}};
   }
-  return plan;
+  // anything else: one compiled kernel; validate with the library's translator
+  std::vector<const char*> b;
+  for (const std::string& x : fused.bodies) b.push_back(x.c_str());
+  size_t need = 0;
+  if (pg_equation_source(b.data(), (int)b.size(), nullptr, 0, &need) != PG_OK)
+    throw std::invalid_argument(std::string("equation set refused: ") + pg_last_error());
+  return {GpuAction{GpuAction::Compiled, "", ""}};
 }
 
 void run_gpu(const FusedEquations& fused, System& sys) {
   for (const GpuAction& a : plan_gpu(fused)) {
     if (a.kind == GpuAction::SphRates) sys.compute_rates();
-    else sys.gather_sum(a.dst, a.src);
+    else if (a.kind == GpuAction::GatherSum) sys.gather_sum(a.dst, a.src);
+    else sys.run_equations(fused.bodies);
   }
 }
 

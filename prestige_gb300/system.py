@@ -168,6 +168,13 @@ class ParticleSystem:
                                                  ctypes.byref(total)), "pg_get_neighbor_list")
         return offs, nbr[:total.value]
 
+    def run_equations(self, bodies):
+        """Run fused pairwise equation bodies (source text) on the GPU over the neighbour set."""
+        if isinstance(bodies, str):
+            bodies = [bodies]
+        arr = (ctypes.c_char_p * len(bodies))(*[b.encode() for b in bodies])
+        nat.check(self._lib.pg_run_equations(self._h, arr, len(bodies)), "pg_run_equations")
+
     def gather_sum(self, dst, src):
         """dst[i] += sum over neighbours j (i included) of src[j]  (eq1 of the reference)."""
         nat.check(self._lib.pg_gather_sum(self._h, dst.encode(), src.encode()), "pg_gather_sum")

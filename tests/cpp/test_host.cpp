@@ -79,11 +79,13 @@ static void test_gpu_plan() {
   CHECK(p.size() == 1 && p[0].kind == GpuAction::GatherSum && p[0].dst == "force" && p[0].src == "mass");
   const std::vector<GpuAction> q = plan_gpu(fuse({sph_continuity(), sph_momentum()}));
   CHECK(q.size() == 1 && q[0].kind == GpuAction::SphRates);
+  const std::vector<GpuAction> c = plan_gpu(fuse({eq1(), equation("odd", "a[i] *= b[j] * r;")}));
+  CHECK(c.size() == 1 && c[0].kind == GpuAction::Compiled);
   bool threw = false;
   try {
-    plan_gpu(fuse({eq1(), equation("odd", "a[i] *= b[j];")}));
-  } catch (const std::invalid_argument&) {
-    threw = true;
+    plan_gpu(fuse({equation("bad", "a[j] += b[i];")}));  // a gather cannot write x[j]
+  } catch (const std::invalid_argument& e) {
+    threw = std::string(e.what()).find("only x[i] may be assigned") != std::string::npos;
   }
   CHECK(threw);
 }
@@ -130,6 +132,26 @@ static void test_gpu_eq1_bit_exact() {
   CHECK(bad == 0);
 }
 
+static void test_gpu_compiled_equations() {
+  const int n = 2000, dim = 3;
+  std::mt19937_64 rng(9);
+  std::uniform_real_distribution<double> U(0.0, 0.2);
+  std::vector<double> pos(n * dim), mass(n, 1.0), a(n, 1.0), c(n, 0.0);
+  for (auto& p : pos) p = U(rng);
+  System sys(sph_config(dim, 0.01, 0.0, 0.2), n);
+  sys.set("pos", pos);
+  sys.set("m2", mass);
+  sys.set("a", a);
+  sys.set("c", c);
+  // two fused bodies: reads of a[j] see the values before the call
+  run_gpu(fuse({equation("e1", "a[i] += m2[j];"), equation("e2", "c[i] += a[j] * 2.0;")}), sys);
+  const std::vector<double> ga = sys.get("a"), gc = sys.get("c");
+  int bad = 0;
+  for (int i = 0; i < n; ++i)
+    if (gc[i] != 2.0 * (ga[i] - 1.0)) ++bad;  // every neighbour has m2 = a = 1
+  CHECK(bad == 0);
+}
+
 static void test_gpu_step_and_adjoint() {
   const int side = 12, n = side * side * side, dim = 3;
   const double dx = 0.01;
@@ -173,6 +195,7 @@ int main(int argc, char** argv) {
     test_gpu_plan();
   } else if (what == "gpu") {
     test_gpu_eq1_bit_exact();
+    test_gpu_compiled_equations();
     test_gpu_step_and_adjoint();
   } else {
     std::fprintf(stderr, "usage: test_host cpu|gpu\n");

@@ -97,6 +97,9 @@ class _FakeSystem:
         self.calls.append(("compute_rates",))
         return "rates"
 
+    def run_equations(self, bodies):
+        self.calls.append(("run_equations", tuple(bodies)))
+
 
 def test_run_gpu_dispatches_eq1_to_the_gather_kernel():
     sysobj = _FakeSystem()
@@ -110,12 +113,22 @@ def test_run_gpu_dispatches_sph_rates():
     assert out == "rates" and sysobj.calls == [("compute_rates",)]
 
 
-def test_run_gpu_refuses_unknown_bodies_without_fallback():
+def test_run_gpu_compiles_general_sets():
     @eqs.equation
     def odd(i, j, a, b):
         a[i] *= b[j]
 
     sysobj = _FakeSystem()
-    with pytest.raises(NotImplementedError):
-        eqs.run_gpu(eqs.fuse([eq1.ir(), odd.ir()]), sysobj)
+    eqs.run_gpu(eqs.fuse([eq1.ir(), odd.ir()]), sysobj)
+    assert sysobj.calls == [("run_equations", ("force[i] += mass[j]", "a[i] *= b[j]"))]
+
+
+def test_run_gpu_refuses_bodies_outside_the_grammar_without_fallback():
+    @eqs.equation
+    def scatter(i, j, a, b):
+        a[j] += b[i]
+
+    sysobj = _FakeSystem()
+    with pytest.raises(ValueError):
+        eqs.run_gpu(eqs.fuse([scatter.ir()]), sysobj)
     assert sysobj.calls == []
