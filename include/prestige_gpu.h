@@ -90,6 +90,7 @@ typedef struct pg_info {
   int grid_n[3];      /* system 0 */
   double grid_lo[3];
   double cell_size;
+  int list_capacity;  /* entries per particle of the pair-pass neighbour lists */
 } pg_info;
 
 /* Fill *cfg with defaults (3D f64 SPH, gamma 7, alpha 0.1, eps 0.01, multiplier 1). */
@@ -134,6 +135,14 @@ int pg_count_neighbors(pg_system* sys, uint32_t* counts);
 /* CSR neighbour lists in traversal order: offsets (n+1), neighbour ids (capacity entries).
  * *total receives the entry count; PG_EOVERFLOW if it exceeds capacity. */
 int pg_get_neighbor_list(pg_system* sys, uint64_t* offsets, uint32_t* neighbors, size_t capacity, size_t* total);
+/* The neighbour lists the SPH pair passes read, as the last step or pg_compute_rates built them
+ * (sorted-slot order of that neighbour search, pg_get_neighbors): slot k has lengths[k] entries,
+ * sorted slots in walk order, at entries[k * list_capacity ...] (min(lengths[k], list_capacity)
+ * of them; the passes walk on for the rest).  In the f64 fast mode they are exactly the
+ * particles within 2h under the f64 test, k itself excluded; in the other modes a superset
+ * that the passes test again.  entries may be null (lengths only); capacity counts u32 entries
+ * and must be at least n * list_capacity (pg_info.list_capacity). */
+int pg_get_pair_lists(pg_system* sys, uint32_t* lengths, uint32_t* entries, size_t capacity);
 
 /* Cell list of n particles that allocates no device memory.  No counterpart in the reference:
  * it exists for callers that cannot call cudaMalloc.  Some hosts give all device memory to an

@@ -44,6 +44,7 @@ class PgInfo(ctypes.Structure):
         ("n_cells", ctypes.c_longlong),
         ("reach", ctypes.c_int), ("pass_grid", ctypes.c_int), ("sort_passes", ctypes.c_int), ("graph", ctypes.c_int),
         ("grid_n", ctypes.c_int * 3), ("grid_lo", _d3), ("cell_size", ctypes.c_double),
+        ("list_capacity", ctypes.c_int),
     ]
 
 
@@ -72,6 +73,7 @@ SIGNATURES = {
     "pg_get_neighbors": (_I, [_P, _P, _P, _P, _SZ]),
     "pg_count_neighbors": (_I, [_P, _P]),
     "pg_get_neighbor_list": (_I, [_P, _P, _P, _SZ, ctypes.POINTER(_SZ)]),
+    "pg_get_pair_lists": (_I, [_P, _P, _P, _SZ]),
     "pg_gather_sum": (_I, [_P, _S, _S]),
     "pg_compute_rates": (_I, [_P]),
     "pg_run_equations": (_I, [_P, ctypes.POINTER(_S), _I]),

@@ -612,12 +612,12 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
   PG_TRY(A->gb.ensure(8 * nn));
   // fast f64 handles: mixed-precision adjoint pair terms; IEEE handles: FP64
   const bool fp32 = s->arith == pg::ARITH_F64_DF;
-  PG_TRY(A->X4.ensure(32 * nn));
-  PG_TRY(A->V4.ensure(32 * nn));
-  PG_TRY(A->Q4.ensure(32 * nn));
-  PG_TRY(A->A4.ensure(32 * nn));
-  PG_TRY(A->PF.ensure(16 * nn));
-  PG_TRY(A->DB.ensure(8 * nn));
+  PG_TRY(A->X4.ensure(32 * (nn + pg::kPackPad)));
+  PG_TRY(A->V4.ensure(32 * (nn + pg::kPackPad)));
+  PG_TRY(A->Q4.ensure(32 * (nn + pg::kPackPad)));
+  PG_TRY(A->A4.ensure(32 * (nn + pg::kPackPad)));
+  PG_TRY(A->PF.ensure(16 * (nn + pg::kPackPad)));
+  PG_TRY(A->DB.ensure(8 * (nn + pg::kPackPad)));
   if (A->pass_grid_fp32 != (int)fp32 || A->pass_grid[pg::SPH_MOM] == 0) {
     int dev = 0, sms = 0;
     PG_CUDA_TRY(cudaGetDevice(&dev));

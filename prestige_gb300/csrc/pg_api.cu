@@ -134,7 +134,7 @@ int ensure_sorted_buffers(pg_system* s) {
   sph_sorted_layout(s->arith, sz);
   const size_t n = s->n ? s->n : 1;
   for (int i = 0; i < 6; ++i)
-    if (sz[i]) PG_TRY(s->sorted[i].ensure(sz[i] * n));
+    if (sz[i]) PG_TRY(s->sorted[i].ensure(sz[i] * (n + kPackPad)));
   PG_TRY(s->nlist.ensure(4 * n * (size_t)s->list_cap));
   PG_TRY(s->nlen.ensure(4 * n));
   PG_TRY(s->nresume.ensure(8 * n));
@@ -207,6 +207,7 @@ int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
   PG_TRY(launch_sph_gather(s->stream, a, s->arith));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[2], s->stream));
   PG_TRY(launch_sph_list(s->stream, a, s->arith, s->list_grid, s->block));
+  s->list_arith = s->arith;
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
   if (rates) {
     PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_RATES, s->pass_grid[SPH_RATES], s->block));
@@ -896,6 +897,31 @@ int pg_get_neighbor_list(pg_system* s, uint64_t* offsets, uint32_t* neighbors, s
   return PG_OK;
 }
 
+int pg_get_pair_lists(pg_system* s, uint32_t* lengths, uint32_t* entries, size_t capacity) {
+  PG_TRY(check(s));
+  if (s->model != PG_MODEL_SPH) {
+    pg::set_error("pair lists exist for SPH systems only");
+    return PG_EINVAL;
+  }
+  if (!lengths) {
+    pg::set_error("null lengths");
+    return PG_EINVAL;
+  }
+  if (s->list_arith < 0 || s->list_arith != s->arith) {
+    pg::set_error("no pair lists for the current arithmetic mode yet (run a step or pg_compute_rates)");
+    return PG_EINVAL;
+  }
+  const size_t n = s->n, need = n * (size_t)s->list_cap;
+  if (entries && capacity < need) {
+    pg::set_error("pair lists need %zu entries (capacity %zu)", need, capacity);
+    return PG_EOVERFLOW;
+  }
+  PG_TRY(pg::sync_and_check(s));
+  if (n) PG_CUDA_TRY(cudaMemcpy(lengths, s->nlen.p, 4 * n, cudaMemcpyDeviceToHost));
+  if (entries && need) PG_CUDA_TRY(cudaMemcpy(entries, s->nlist.p, 4 * need, cudaMemcpyDeviceToHost));
+  return PG_OK;
+}
+
 int pg_gather_sum(pg_system* s, const char* dst, const char* src) {
   PG_TRY(check(s));
   if (!dst || !src) {
@@ -1082,6 +1108,7 @@ int pg_get_info(pg_system* s, pg_info* info) {
   }
   info->cell_size = s->grids[0].cell;
   info->graph = s->graph_enabled ? 1 : 0;
+  info->list_capacity = s->list_cap;
   return PG_OK;
 }
 

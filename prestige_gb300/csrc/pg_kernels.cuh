@@ -15,8 +15,10 @@ enum Arith {
   ARITH_F32_FAST = 3,   // single precision with fused multiply-add
 };
 
-constexpr int kSphThreads = 128;     // block size of the two-phase pass and the default
+constexpr int kSphThreads = 128;     // default block size of the SPH kernels
 constexpr int kSphMaxThreads = 256;  // largest block size of the list-based kernels
+constexpr size_t kPackPad = 8;       // records allocated past the end of every sorted pack: the
+                                     // list kernel's batched loads may run up to 3 past a row
 
 // Stages of the SPH pair pass.
 enum SphStage {
@@ -75,8 +77,6 @@ struct SphArgs {
 };
 
 int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith);
-int launch_sph_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid);
-int sph_pass_occupancy(int arith, int dim, int stage);
 // Neighbour lists for the list-based passes (stage passes read a.nlist / a.nlen / a.nresume).
 // block: threads per block (multiple of 32, <= kSphMaxThreads).
 int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid, int block);

@@ -227,7 +227,7 @@ struct DfPairs {
   const double4_32a* Xd;
   SphDF w;
   double four_h2;
-  double xid[3];
+  uint32_t kself;
   df xi[3], vi[3], rhoi, Pi;
   dfacc acc[3], dr;
 
@@ -249,38 +249,45 @@ struct DfPairs {
       rhoi = df_make(rp.x, rp.y);
       Pi = df_make(rp.z, rp.w);
     }
-    const double4_32a xd = Xd[k];
-    xid[0] = xd.x; xid[1] = xd.y; xid[2] = xd.z;
+    kself = k;
     acc[0] = acc[1] = acc[2] = dfacc_zero();
     dr = dfacc_zero();
   }
 
-  // The oracle's f64 neighbour test, used only when the double-word r^2 is within a relative
-  // band of 1e-9 of (2h)^2 (never, in practice).
-  __device__ __noinline__ bool exact_test(uint32_t t) const {
-    const double4_32a xj = Xd[t];
-    const double d0 = __dsub_rn(xid[0], xj.x), d1 = __dsub_rn(xid[1], xj.y);
-    double r2 = __dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1));
-    if (DIM == 3) {
-      const double d2 = __dsub_rn(xid[2], xj.z);
-      r2 = __dadd_rn(r2, __dmul_rn(d2, d2));
-    }
-    return r2 < four_h2 && r2 > 0.0;
+  // Geometry of pair (k, t): x_ij, r^2, F = (dW/dr)/r and w = v_ij . x_ij.  CHECK: false when t is
+  // not a neighbour (outside the support, or t == k), the oracle's f64 test deciding when the
+  // double-word r^2 is within a relative band of 1e-9 of (2h)^2.  Without CHECK, t comes from an
+  // exact neighbour list (sph_list_kernel with f64 classification).
+  // The sorted-pack records of one neighbour, loaded ahead of its pair terms.
+  struct Pre {
+    float4 ah, al, bh, bl, rp;
+  };
+  static constexpr bool kPrefetch = true;
+
+  __device__ __forceinline__ Pre fetch(uint32_t t) const {
+    Pre p;
+    p.ah = Ah[t];
+    p.al = Al[t];
+    p.bh = Bh[t];
+    p.bl = Bl[t];
+    p.rp = kMom ? RP[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+    return p;
   }
 
-  // Geometry of pair (k, t): x_ij, r^2, F = (dW/dr)/r and w = v_ij . x_ij.  False when t is not
-  // a neighbour (outside the support, or t == k).
-  __device__ __forceinline__ bool geometry(uint32_t t, df* d, df& r2, df& F, df& wv, df& mj) const {
-    const float4 ah = Ah[t], al = Al[t];
+  template <bool CHECK>
+  __device__ __forceinline__ bool geometry(uint32_t t, const Pre& p, df* d, df& r2, df& F, df& wv, df& mj) const {
+    const float4 ah = p.ah, al = p.al;
     d[0] = df_sub(xi[0], df_make(ah.x, al.x));
     d[1] = df_sub(xi[1], df_make(ah.y, al.y));
     d[2] = DIM == 3 ? df_sub(xi[2], df_make(ah.z, al.z)) : df_make(0.f, 0.f);
     r2 = df_sumsq3(d[0], d[1], d[2]);
-    const df gap = df_sub(r2, df_make(w.four_h2[0], w.four_h2[1]));
-    if (fabsf(gap.hi) <= w.band) {
-      if (!exact_test(t)) return false;
-    } else if (!(gap.hi < 0.f)) {
-      return false;
+    if (CHECK) {
+      const df gap = df_sub(r2, df_make(w.four_h2[0], w.four_h2[1]));
+      if (fabsf(gap.hi) <= w.band) {
+        if (!exact_neighbor_call<DIM>(Xd, kself, t, four_h2)) return false;
+      } else if (!(gap.hi < 0.f)) {
+        return false;
+      }
     }
     if (!(r2.hi > 0.f)) return false;
     const df inv_r = df_rsqrt(r2);
@@ -292,7 +299,7 @@ struct DfPairs {
       const df tq = df_add_f(df_neg(q), 2.0f);
       F = df_mul(df_mul(df_make(w.fb[0], w.fb[1]), df_mul(tq, tq)), inv_r);
     }
-    const float4 bh = Bh[t], bl = Bl[t];
+    const float4 bh = p.bh, bl = p.bl;
     const df dv0 = df_sub(vi[0], df_make(bh.x, bl.x));
     const df dv1 = df_sub(vi[1], df_make(bh.y, bl.y));
     const df dv2 = DIM == 3 ? df_sub(vi[2], df_make(bh.z, bl.z)) : df_make(0.f, 0.f);
@@ -301,8 +308,7 @@ struct DfPairs {
     return true;
   }
 
-  __device__ __forceinline__ void momentum(uint32_t t, const df* d, df r2, df F, df wv, df mj) {
-    const float4 rpj = RP[t];
+  __device__ __forceinline__ void momentum(const float4& rpj, const df* d, df r2, df F, df wv, df mj) {
     df pij = df_make(0.f, 0.f);
     if (wv.hi < 0.f) {
       const df den = df_mul(df_add(r2, df_make(w.eps_h2[0], w.eps_h2[1])), df_add(rhoi, df_make(rpj.x, rpj.y)));
@@ -314,12 +320,18 @@ struct DfPairs {
     if (DIM == 3) dfacc_add_prod(acc[2], ncoef, d[2]);
   }
 
-  __device__ __forceinline__ void pair(uint32_t t) {
+  template <bool CHECK>
+  __device__ __forceinline__ void terms(uint32_t t, const Pre& p) {
     df d[3], r2, F, wv, mj;
-    if (!geometry(t, d, r2, F, wv, mj)) return;
+    if (!geometry<CHECK>(t, p, d, r2, F, wv, mj)) return;
     if (kCont) dfacc_add_prod(dr, mj, df_mul(wv, F));
-    if (kMom) momentum(t, d, r2, F, wv, mj);
+    if (kMom) momentum(p.rp, d, r2, F, wv, mj);
   }
+
+  // an entry of an exact neighbour list
+  __device__ __forceinline__ void pair_with(uint32_t t, const Pre& p) { terms<false>(t, p); }
+  // any candidate (the walk that continues an overflowed list)
+  __device__ __forceinline__ void pair(uint32_t t) { terms<true>(t, fetch(t)); }
 
   __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id, uint32_t k) {
     const SphC<double>& c = K.d;
@@ -351,41 +363,7 @@ struct DfPairs {
 // ---------------------------------------------------------------------------------------
 typedef void (*PassKernel)(SphArgs, int);
 
-template <int DIM, int STAGE>
-PassKernel pass_kernel_for(int arith, int* pf_index) {
-  switch (arith) {
-    case ARITH_F64_EXACT:
-      *pf_index = 3;
-      return sph_pass_kernel<RealPairs<OpsD, DIM, true, STAGE>, DIM, false>;
-    case ARITH_F64_DF:
-      *pf_index = 0;
-      return sph_pass_kernel<DfPairs<DIM, STAGE>, DIM, false>;
-    case ARITH_F32_EXACT:
-      *pf_index = 0;
-      return sph_pass_kernel<RealPairs<OpsF, DIM, false, STAGE>, DIM, true>;
-    case ARITH_F32_FAST:
-      *pf_index = 0;
-      return sph_pass_kernel<RealPairs<OpsFF, DIM, false, STAGE>, DIM, true>;
-    default:
-      return nullptr;
-  }
-}
-
-template <int DIM>
-PassKernel pass_kernel_dim(int arith, int stage, int* pf_index) {
-  switch (stage) {
-    case SPH_RATES: return pass_kernel_for<DIM, SPH_RATES>(arith, pf_index);
-    case SPH_CONT: return pass_kernel_for<DIM, SPH_CONT>(arith, pf_index);
-    case SPH_MOM: return pass_kernel_for<DIM, SPH_MOM>(arith, pf_index);
-    default: return nullptr;
-  }
-}
-
-PassKernel pass_kernel(int arith, int dim, int stage, int* pf_index) {
-  return dim == 2 ? pass_kernel_dim<2>(arith, stage, pf_index) : pass_kernel_dim<3>(arith, stage, pf_index);
-}
-
-// The same table for the list-based passes and the list kernel (stage < 0).
+// Kernel table for the list-based passes and the list kernel (stage < 0).
 template <int DIM, int STAGE>
 PassKernel list_pass_for(int arith, int* pf_index) {
   switch (arith) {
@@ -417,14 +395,14 @@ PassKernel list_kernel_dim(int arith, int stage, int* pf_index) {
   switch (arith) {  // the list kernel
     case ARITH_F64_EXACT:
       *pf_index = 3;
-      return sph_list_kernel<DIM, false>;
-    case ARITH_F64_DF:
+      return sph_list_kernel<DIM, false, -1>;
+    case ARITH_F64_DF:  // exact lists: the double-word passes skip the neighbour test
       *pf_index = 0;
-      return sph_list_kernel<DIM, false>;
+      return sph_list_kernel<DIM, false, 5>;
     case ARITH_F32_EXACT:
     case ARITH_F32_FAST:
       *pf_index = 0;
-      return sph_list_kernel<DIM, true>;
+      return sph_list_kernel<DIM, true, -1>;
     default:
       return nullptr;
   }
@@ -497,21 +475,6 @@ int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith) {
   return PG_OK;
 }
 
-int launch_sph_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid) {
-  int pf = 0;
-  PassKernel kern = pass_kernel(arith, a.dim, stage, &pf);
-  if (!kern) {
-    set_error("unknown arithmetic mode %d or stage %d", arith, stage);
-    return PG_EINVAL;
-  }
-  if (a.n == 0) return PG_OK;
-  const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
-  if (grid <= 0 || (uint32_t)grid > ntiles) grid = (int)ntiles;
-  kern<<<grid, kSphThreads, 0, st>>>(a, pf);
-  PG_CUDA_TRY(cudaGetLastError());
-  return PG_OK;
-}
-
 int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid, int block) {
   int pf = 0;
   PassKernel kern = list_kernel(arith, a.dim, -1, &pf);
@@ -519,7 +482,7 @@ int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid, int 
 }
 
 int launch_sph_list_pf(cudaStream_t st, const SphArgs& a, int pf_index, int grid, int block) {
-  PassKernel kern = a.dim == 2 ? sph_list_kernel<2, false> : sph_list_kernel<3, false>;
+  PassKernel kern = a.dim == 2 ? sph_list_kernel<2, false, -1> : sph_list_kernel<3, false, -1>;
   return launch_table(st, a, kern, pf_index, grid, block);
 }
 
@@ -534,14 +497,6 @@ int sph_list_occupancy(int arith, int dim, int stage, int block) {
   PassKernel kern = list_kernel(arith, dim, stage, &pf);
   if (!kern) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, block, 0) != cudaSuccess) return 0;
-  return blocks;
-}
-
-int sph_pass_occupancy(int arith, int dim, int stage) {
-  int pf = 0, blocks = 0;
-  PassKernel kern = pass_kernel(arith, dim, stage, &pf);
-  if (!kern) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, kSphThreads, 0) != cudaSuccess) return 0;
   return blocks;
 }
 

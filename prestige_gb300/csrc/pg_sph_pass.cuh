@@ -1,7 +1,7 @@
-// The SPH pair-pass skeleton shared by the forward pass (pg_sph.cu) and the adjoint pass
-// (pg_adjoint.cu): one thread per target slot, a two-phase candidate walk over the neighbour
-// rows (cheap FP32 filter into a per-thread hit list in shared memory, then the exact test and
-// the pair terms of a `Pairs` policy over the listed hits), and the Tait pressure term.
+// The SPH pair-pass skeleton shared by the forward passes (pg_sph.cu) and the adjoint passes
+// (pg_adjoint.cu): the candidate walk over the neighbour rows with its FP32 prefilter, the
+// neighbour-list kernel built on it, the list-driven pair pass (one thread per target slot) and
+// the Tait pressure term.
 //
 // A `Pairs` policy provides
 //   begin(args, system, slot)   load the target's data
@@ -18,8 +18,6 @@
 namespace pg {
 namespace sphpass {
 
-constexpr int kHitCap = 32;
-constexpr unsigned kFull = 0xffffffffu;
 
 template <class R> struct V4;
 template <> struct V4<double> { typedef double4_32a T; };
@@ -103,81 +101,112 @@ __device__ __forceinline__ bool prefilter_hit(const float4& pi, const float4& pj
   return r2 < thr;
 }
 
-// ---------------------------------------------------------------------------------------
-// The two-phase pass (candidate walk and pair terms in one kernel).  PF: the FP32 position
-// array tested in phase 1 (float4 x,y,z per slot).
-// ---------------------------------------------------------------------------------------
-template <class Pairs, int DIM, bool EXACT_PF>
-__global__ void __launch_bounds__(kSphThreads) sph_pass_kernel(SphArgs a, int pf_index) {
-  __shared__ uint32_t hits[kHitCap][kSphThreads];
-  const int tid = threadIdx.x;
-  const float4* __restrict__ PF = (const float4*)a.s[pf_index];
-  const uint32_t* __restrict__ start = a.cell_start;
-  const int R = a.reach;
-  const int RZ = DIM == 3 ? R : 0;
-  const int side = 2 * R + 1;
-  const int nrows = side * (2 * RZ + 1);
-  const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
+// FP32 r^2 below which |x_j - x_i| < 2h holds in f64 for certain: the mirror image of
+// prefilter_threshold (same error bound delta, taken off instead of added).
+__device__ __forceinline__ float certain_threshold(const SphK& K, const float4& pi) {
+  const float M = fmaxf(fmaxf(fabsf(pi.x), fabsf(pi.y)), fabsf(pi.z)) + K.two_h_f;
+  const float delta = 2.384185791015625e-07f * (2.f * M + K.two_h_f);
+  const float rr = fmaxf(K.two_h_f - 2.f * delta, 0.f);
+  return rr * rr * 0.9999847f;
+}
 
-  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const SphK* Kp;
-    const Target T = target_of(a, tile * kSphThreads + tid, &Kp, R);
-    const SphK& K = *Kp;
-    const GridK& g = K.g;
+// The oracle's f64 neighbour test of slots k and t (positions X, double4 per slot); inline in
+// the list kernel, called out of line by the pair passes (exact_neighbor_call), where the f64
+// registers would otherwise count against the pair loop.
+template <int DIM>
+__device__ __forceinline__ bool exact_neighbor(const double4_32a* X, uint32_t k, uint32_t t, double four_h2) {
+  const double4_32a xi = X[k], xj = X[t];
+  const double d0 = __dsub_rn(xi.x, xj.x), d1 = __dsub_rn(xi.y, xj.y);
+  double r2 = __dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1));
+  if (DIM == 3) {
+    const double d2 = __dsub_rn(xi.z, xj.z);
+    r2 = __dadd_rn(r2, __dmul_rn(d2, d2));
+  }
+  return r2 < four_h2 && r2 > 0.0;
+}
 
-    Pairs P;
-    P.begin(a, K, T.k);
-    const float4 pi = PF[T.k];
-    const float thr = prefilter_threshold<EXACT_PF>(K, pi);
+template <int DIM>
+__device__ __noinline__ bool exact_neighbor_call(const double4_32a* X, uint32_t k, uint32_t t, double four_h2) {
+  return exact_neighbor<DIM>(X, k, t, four_h2);
+}
 
-    int nh = 0;
-    int row = 0;
-    uint32_t t = 0, e = 0;
-    while (true) {
-      // advance this lane to its next candidate (rows z, y ascending)
-      while (t >= e && row < nrows) {
-        const int dz = row / side - RZ, dy = row % side - R;
-        ++row;
-        const int z = T.cz + dz, y = T.cy + dy;
-        if (!T.live || z < 0 || z >= g.nz || y < 0 || y >= g.ny) continue;
-        const uint32_t rb = g.cell_base + ((uint32_t)z * g.ny + (uint32_t)y) * g.nx;
-        t = start[rb + T.x0];
-        e = start[rb + T.x1 + 1];
-      }
-      const bool has = t < e;
-      if (has) {
-        if (prefilter_hit<DIM, EXACT_PF>(pi, PF[t], thr)) hits[nh++][tid] = t;
-        ++t;
-      }
-      const bool done = !__any_sync(kFull, has);
-      if (done || __any_sync(kFull, nh == kHitCap)) {
-        for (int h = 0; __any_sync(kFull, h < nh); ++h)
-          if (h < nh) P.pair(hits[h][tid]);
-        nh = 0;
-        if (done) break;
-      }
+// FP32 r^2 of a candidate, in the operation order of the prefilter (EXACT_PF: IEEE single, no
+// contraction; otherwise with fused multiply-add).
+template <int DIM, bool EXACT_PF>
+__device__ __forceinline__ float candidate_r2(const float4& pi, const float4& pj) {
+  if (EXACT_PF) {
+    const float d0 = __fsub_rn(pi.x, pj.x), d1 = __fsub_rn(pi.y, pj.y);
+    float r2 = __fadd_rn(__fmul_rn(d0, d0), __fmul_rn(d1, d1));
+    if (DIM == 3) {
+      const float d2 = __fsub_rn(pi.z, pj.z);
+      r2 = __fadd_rn(r2, __fmul_rn(d2, d2));
     }
-    if (T.live) P.finish(a, K, T.id, T.k);
+    return r2;
+  }
+  const float d0 = pi.x - pj.x, d1 = pi.y - pj.y;
+  float r2 = fmaf(d1, d1, d0 * d0);
+  if (DIM == 3) {
+    const float d2 = pi.z - pj.z;
+    r2 = fmaf(d2, d2, r2);
+  }
+  return r2;
+}
+
+// List membership of a candidate for target k (t != k is tested by the caller).  XD < 0: the FP32
+// prefilter (hit; a superset of the neighbours, the pair passes repeat the exact test).
+// XD >= 0: exactly the oracle's f64 test.  hit: a neighbour for certain; below: under the
+// conservative threshold.  Candidates below but not hit (a narrow band around (2h)^2, and
+// coincident FP32 positions) are left to exact_neighbor on the f64 positions a.s[XD].
+template <int DIM, bool EXACT_PF, int XD>
+__device__ __forceinline__ void classify(const float4& pi, const float4& pj, float thr, float thr_lo, bool& hit,
+                                         bool& below) {
+  const float r2 = candidate_r2<DIM, EXACT_PF>(pi, pj);
+  if (XD < 0) {
+    hit = r2 < thr && (!EXACT_PF || r2 > 0.f);
+    below = false;
+  } else {
+    hit = r2 < thr_lo && r2 > 0.f;
+    below = r2 < thr;
   }
 }
 
 // ---------------------------------------------------------------------------------------
-// Neighbour lists.  sph_list_kernel walks the candidates of every slot once per step (the
-// same concatenated walk and FP32 prefilter as above) and writes the passing slots, in
-// traversal order, to nlist[k * cap ...]; nlen[k] = number of passing slots (may exceed cap).
-// When the list fills, nresume[2k], [2k+1] = (row, slot) of the first passing candidate that
-// did not fit, so the pair passes can continue the walk from there.
+// Neighbour lists.  sph_list_kernel walks the candidates of every slot once per step and writes
+// the listed slots (classify: the FP32 superset, or with XD >= 0 exactly the f64 neighbours;
+// never the slot itself) in walk order (rows z, then y ascending; slots ascending along a row)
+// to nlist[k * cap ...]; nlen[k] = number of listed slots (may exceed cap).  When the list fills,
+// nresume[2k], [2k+1] = (row, slot) of the first listed candidate that did not fit, so the pair
+// passes can continue the walk from there.
+//
+// Each lane walks its own rows, kListBatch candidates at a time: loads without a clamp (the packs are padded by kPackPad records), the
+// FP32 classification folded into bit masks, the rare f64 band tests once per batch, then the
+// pushes of the batch's hits in order.  Lanes whose targets share a cell walk the same
+// candidates in step, so their loads coalesce (pruning each lane's rows to the cells its own
+// target can reach was measured: it breaks that, and the walk got slower).
 // ---------------------------------------------------------------------------------------
-template <int DIM, bool EXACT_PF>
+constexpr int kListBatch = 8;
+
+__device__ __forceinline__ void list_push(const SphArgs& a, uint32_t* my, uint32_t& cnt, uint32_t k, int row,
+                                          uint32_t t) {
+  if (cnt < a.cap) {
+    my[cnt] = t;
+  } else if (cnt == a.cap) {
+    a.nresume[2 * (size_t)k] = (uint32_t)row;
+    a.nresume[2 * (size_t)k + 1] = t;
+  }
+  ++cnt;
+}
+
+template <int DIM, bool EXACT_PF, int XD>
 __global__ void __launch_bounds__(kSphMaxThreads) sph_list_kernel(SphArgs a, int pf_index) {
   const int tid = threadIdx.x;
   const float4* __restrict__ PF = (const float4*)a.s[pf_index];
+  const double4_32a* __restrict__ X = (const double4_32a*)a.s[XD < 0 ? 0 : XD];
   const uint32_t* __restrict__ start = a.cell_start;
   const int R = a.reach;
   const int RZ = DIM == 3 ? R : 0;
   const int side = 2 * R + 1;
   const int nrows = side * (2 * RZ + 1);
-  const uint32_t cap = a.cap;
   const uint32_t bs = blockDim.x;
   const uint32_t ntiles = (a.n + bs - 1) / bs;
 
@@ -188,7 +217,8 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_kernel(SphArgs a, int
     const GridK& g = K.g;
     const float4 pi = PF[T.k];
     const float thr = prefilter_threshold<EXACT_PF>(K, pi);
-    uint32_t* __restrict__ my = a.nlist + (size_t)T.k * cap;
+    const float thr_lo = XD < 0 ? 0.f : certain_threshold(K, pi);
+    uint32_t* __restrict__ my = a.nlist + (size_t)T.k * a.cap;
     uint32_t cnt = 0;
     int row = 0;
     uint32_t t = 0, e = 0;
@@ -202,23 +232,46 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_kernel(SphArgs a, int
         t = start[rb + T.x0];
         e = start[rb + T.x1 + 1];
       }
-      if (!__any_sync(kFull, t < e)) break;
-      if (t < e) {
-        if (prefilter_hit<DIM, EXACT_PF>(pi, PF[t], thr)) {
-          if (cnt < cap) {
-            my[cnt] = t;
-          } else if (cnt == cap) {
-            a.nresume[2 * (size_t)T.k] = (uint32_t)(row - 1);
-            a.nresume[2 * (size_t)T.k + 1] = t;
-          }
-          ++cnt;
-        }
-        ++t;
+      if (t >= e) break;
+      // the batch's candidates that belong to the row, the target itself left out (the packs
+      // are padded by kPackPad records, so the loads need no clamp)
+      unsigned valid = e - t >= (uint32_t)kListBatch ? (1u << kListBatch) - 1 : (1u << (e - t)) - 1;
+      if (T.k - t < (uint32_t)kListBatch) valid &= ~(1u << (T.k - t));
+      const float4* __restrict__ pb = PF + t;
+      float4 pj[kListBatch];
+#pragma unroll
+      for (int b = 0; b < kListBatch; ++b) pj[b] = __ldg(pb + b);
+      unsigned hit = 0, below = 0;
+#pragma unroll
+      for (int b = 0; b < kListBatch; ++b) {
+        bool h, m;
+        classify<DIM, EXACT_PF, XD>(pi, pj[b], thr, thr_lo, h, m);
+        if (h) hit |= 1u << b;
+        if (m) below |= 1u << b;
       }
+      hit &= valid;
+      if (XD >= 0) {
+        for (unsigned m = below & ~hit & valid; m; m &= m - 1) {
+          const int b = __ffs(m) - 1;
+          if (exact_neighbor<DIM>(X, T.k, t + b, K.d.four_h2)) hit |= 1u << b;
+        }
+      }
+      for (; hit; hit &= hit - 1) list_push(a, my, cnt, T.k, row - 1, t + __ffs(hit) - 1);
+      t += kListBatch;
     }
     if (T.live) a.nlen[T.k] = cnt;
   }
 }
+
+// Policies that split a pair into fetch(t) (the neighbour's loads) and pair_with(t, fetched).
+template <class P, class = void>
+struct PrefetchPolicy {
+  static constexpr bool value = false;
+};
+template <class P>
+struct PrefetchPolicy<P, decltype((void)P::kPrefetch)> {
+  static constexpr bool value = P::kPrefetch;
+};
 
 // Pair pass over the lists of sph_list_kernel (any block size up to kSphMaxThreads, a
 // multiple of 32).  Lanes step through their lists together;
@@ -240,7 +293,22 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_pass_kernel(SphArgs a
     const uint32_t cnt = live ? a.nlen[k] : 0u;
     const uint32_t L = min(cnt, cap);
     const uint32_t* __restrict__ my = a.nlist + (size_t)k * cap;
-    for (uint32_t q = 0; q < L; ++q) P.pair(my[q]);
+    if constexpr (PrefetchPolicy<Pairs>::value) {
+      // software pipeline: list entries two ahead, the neighbour's pack records one ahead
+      uint32_t t = L ? my[0] : k;
+      uint32_t tn = L > 1 ? my[1] : t;
+      typename Pairs::Pre cur = P.fetch(t);
+      for (uint32_t q = 0; q < L; ++q) {
+        const uint32_t tnn = q + 2 < L ? my[q + 2] : tn;
+        const typename Pairs::Pre nxt = P.fetch(tn);
+        P.pair_with(t, cur);
+        cur = nxt;
+        t = tn;
+        tn = tnn;
+      }
+    } else {
+      for (uint32_t q = 0; q < L; ++q) P.pair(my[q]);
+    }
     if (cnt > cap) {
       // rare: continue the candidate walk where the list stopped
       const float4* __restrict__ PF = (const float4*)a.s[pf_index];

@@ -63,6 +63,7 @@ struct pg_system {
 
   // CUDA graph of one step (DEM: one per history parity)
   bool graph_enabled = false;
+  int list_arith = -1;  // arithmetic mode of the pair lists in nlist/nlen (-1: none built yet)
   cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
 
   // step timing (pg_timing_enable): 4 events per step, consumed by pg_timing_read

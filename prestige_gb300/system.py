@@ -168,6 +168,17 @@ class ParticleSystem:
                                                  ctypes.byref(total)), "pg_get_neighbor_list")
         return offs, nbr[:total.value]
 
+    def pair_lists(self):
+        """(lengths, entries) of the pair-pass neighbour lists built by the last step or
+        compute_rates: per sorted slot, lengths[k] and entries[k, :min(lengths[k], cap)]
+        (sorted slots)."""
+        cap = self.info()["list_capacity"]
+        lengths = np.empty(self.n, np.uint32)
+        entries = np.empty((self.n, cap), np.uint32)
+        nat.check(self._lib.pg_get_pair_lists(self._h, lengths.ctypes.data, entries.ctypes.data, entries.size),
+                  "pg_get_pair_lists")
+        return lengths, entries
+
     def run_equations(self, bodies):
         """Run fused pairwise equation bodies (source text) on the GPU over the neighbour set."""
         if isinstance(bodies, str):
