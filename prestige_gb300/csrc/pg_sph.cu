@@ -88,6 +88,12 @@ __device__ __forceinline__ float4 df_pack_rho_p(double rho, double P) {
   return r;
 }
 
+// The pair passes' per-slot record in the double-word mode: positions and mass (hi, lo) and
+// velocities (hi, lo), 64 bytes, so the four loads of a neighbour touch two sectors of one line.
+struct __align__(64) DfRecord {
+  float4 ah, al, bh, bl;
+};
+
 template <int DIM>
 __global__ void sph_gather_df(SphArgs a) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -114,9 +120,12 @@ __global__ void sph_gather_df(SphArgs a) {
   df_split(v[2], &bh.z, &bl.z);
   bh.w = bl.w = 0.f;
   ((float4*)a.s[0])[k] = ah;
-  ((float4*)a.s[1])[k] = al;
-  ((float4*)a.s[2])[k] = bh;
-  ((float4*)a.s[3])[k] = bl;
+  DfRecord rec;
+  rec.ah = ah;
+  rec.al = al;
+  rec.bh = bh;
+  rec.bl = bl;
+  ((DfRecord*)a.s[1])[k] = rec;
   ((float4*)a.s[4])[k] = df_pack_rho_p(rho, tait_pterm<OpsD>(K.d, K.gamma, rho));
   ((double4_32a*)a.s[5])[k] = make_double4_32a(x[0], x[1], x[2], 0.0);
 }
@@ -223,7 +232,8 @@ template <int DIM, int STAGE>
 struct DfPairs {
   static constexpr bool kCont = STAGE != SPH_MOM;
   static constexpr bool kMom = STAGE != SPH_CONT;
-  const float4 *Ah, *Al, *Bh, *Bl, *RP;
+  const DfRecord* Rec;
+  const float4* RP;
   const double4_32a* Xd;
   SphDF w;
   double four_h2;
@@ -232,15 +242,12 @@ struct DfPairs {
   dfacc acc[3], dr;
 
   __device__ __forceinline__ void begin(const SphArgs& a, const SphK& K, uint32_t k) {
-    Ah = (const float4*)a.s[0];
-    Al = (const float4*)a.s[1];
-    Bh = (const float4*)a.s[2];
-    Bl = (const float4*)a.s[3];
+    Rec = (const DfRecord*)a.s[1];
     RP = (const float4*)a.s[4];
     Xd = (const double4_32a*)a.s[5];
     w = K.w;
     four_h2 = K.d.four_h2;
-    const float4 ah = Ah[k], al = Al[k], bh = Bh[k], bl = Bl[k];
+    const float4 ah = Rec[k].ah, al = Rec[k].al, bh = Rec[k].bh, bl = Rec[k].bl;
     xi[0] = df_make(ah.x, al.x); xi[1] = df_make(ah.y, al.y); xi[2] = df_make(ah.z, al.z);
     vi[0] = df_make(bh.x, bl.x); vi[1] = df_make(bh.y, bl.y); vi[2] = df_make(bh.z, bl.z);
     rhoi = Pi = df_make(0.f, 0.f);
@@ -266,10 +273,10 @@ struct DfPairs {
 
   __device__ __forceinline__ Pre fetch(uint32_t t) const {
     Pre p;
-    p.ah = Ah[t];
-    p.al = Al[t];
-    p.bh = Bh[t];
-    p.bl = Bl[t];
+    p.ah = Rec[t].ah;
+    p.al = Rec[t].al;
+    p.bh = Rec[t].bh;
+    p.bl = Rec[t].bl;
     p.rp = kMom ? RP[t] : make_float4(0.f, 0.f, 0.f, 0.f);
     return p;
   }
@@ -437,8 +444,9 @@ void sph_sorted_layout(int arith, size_t sz[6]) {
     case ARITH_F64_EXACT:  // double4 {x,m}, double4 {v,0}, double2 {rho,P}, float4 prefilter positions
       sz[0] = 32; sz[1] = 32; sz[2] = 16; sz[3] = 16;
       break;
-    case ARITH_F64_DF:  // float4 A.hi, A.lo, V.hi, V.lo, float4 {rho, P} (hi, lo), double4 exact positions
-      sz[0] = 16; sz[1] = 16; sz[2] = 16; sz[3] = 16; sz[4] = 16; sz[5] = 32;
+    case ARITH_F64_DF:  // float4 A.hi (list kernel), DfRecord {A.hi, A.lo, V.hi, V.lo} (pair passes),
+                        // float4 {rho, P} (hi, lo), double4 exact positions
+      sz[0] = 16; sz[1] = 64; sz[4] = 16; sz[5] = 32;
       break;
     default:  // float4 {x,m}, float4 {v,0}, float2 {rho,P}
       sz[0] = 16; sz[1] = 16; sz[2] = 8;

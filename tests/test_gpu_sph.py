@@ -185,8 +185,8 @@ def test_list_overflow_continues_the_walk(pg, oracle, cap, precision, mode):
 
 @pytest.mark.parametrize("mult", [0.4, 0.5, 1.0])
 def test_steps_bit_exact_across_cell_sizes(pg, oracle, mult):
-    """Neighbour rows staged in shared memory (reach 1 and 2) and the global walk (reach 3)
-    give the oracle's results for the same cell multiplier."""
+    """The neighbour lists and pair passes give the oracle's results for cell multipliers with
+    reach 1, 2 and 3 (cell sizes 2h, h and 0.8h)."""
     w = workloads.sph_lattice_3d(n=4000, seed=41, cell_multiplier=mult)
     s, cfg = _pair(w, 1, 0)
     st = _ostate(oracle, w)
