@@ -135,7 +135,7 @@ int ensure_sorted_buffers(pg_system* s) {
   const size_t n = s->n ? s->n : 1;
   for (int i = 0; i < 6; ++i)
     if (sz[i]) PG_TRY(s->sorted[i].ensure(sz[i] * (n + kPackPad)));
-  PG_TRY(s->nlist.ensure(4 * n * (size_t)s->list_cap));
+  PG_TRY(s->nlist.ensure(4 * ((n + kListTile - 1) / kListTile) * kListTile * (size_t)s->list_cap));
   PG_TRY(s->nlen.ensure(4 * n));
   PG_TRY(s->nresume.ensure(8 * n));
   return PG_OK;
@@ -912,13 +912,20 @@ int pg_get_pair_lists(pg_system* s, uint32_t* lengths, uint32_t* entries, size_t
     return PG_EINVAL;
   }
   const size_t n = s->n, need = n * (size_t)s->list_cap;
+  const size_t stored = (n + pg::kListTile - 1) / pg::kListTile * pg::kListTile * (size_t)s->list_cap;
   if (entries && capacity < need) {
     pg::set_error("pair lists need %zu entries (capacity %zu)", need, capacity);
     return PG_EOVERFLOW;
   }
   PG_TRY(pg::sync_and_check(s));
   if (n) PG_CUDA_TRY(cudaMemcpy(lengths, s->nlen.p, 4 * n, cudaMemcpyDeviceToHost));
-  if (entries && need) PG_CUDA_TRY(cudaMemcpy(entries, s->nlist.p, 4 * need, cudaMemcpyDeviceToHost));
+  if (entries && need) {  // the device lists are tiled by 32 slots; the caller gets them slot by slot
+    std::vector<uint32_t> tiled(stored);
+    PG_CUDA_TRY(cudaMemcpy(tiled.data(), s->nlist.p, 4 * stored, cudaMemcpyDeviceToHost));
+    const size_t cap = (size_t)s->list_cap, T = pg::kListTile;
+    for (size_t k = 0; k < n; ++k)
+      for (size_t q = 0; q < cap; ++q) entries[k * cap + q] = tiled[(k / T) * cap * T + q * T + k % T];
+  }
   return PG_OK;
 }
 

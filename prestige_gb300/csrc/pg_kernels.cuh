@@ -17,6 +17,7 @@ enum Arith {
 
 constexpr int kSphThreads = 128;     // default block size of the SPH kernels
 constexpr int kSphMaxThreads = 256;  // largest block size of the list-based kernels
+constexpr uint32_t kListTile = 32;  // slots per tile of the neighbour-list array
 constexpr size_t kPackPad = 8;       // records allocated past the end of every sorted pack: the
                                      // list kernel's batched loads may run up to 3 past a row
 
@@ -68,7 +69,8 @@ struct SphArgs {
   void* drho;
   void* lam[5];              // adjoint (pg_adjoint.cu): lambda_x, lambda_v, lambda_rho, dL/dalpha and
                              // dL/dB partial sums, all id order
-  uint32_t* nlist;           // neighbour lists, slot order: nlist[k * cap + q] (q < min(nlen[k], cap))
+  uint32_t* nlist;           // neighbour lists in tiles of kListTile slots: entry q of slot k at
+                             // nlist[(k / 32) * cap * 32 + q * 32 + k % 32] (q < min(nlen[k], cap))
   uint32_t* nlen;            // neighbours of slot k that passed the prefilter (may exceed cap)
   uint32_t* nresume;         // (row, slot) where the walk continues when nlen[k] > cap
   uint32_t cap;

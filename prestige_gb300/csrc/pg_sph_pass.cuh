@@ -186,10 +186,15 @@ __device__ __forceinline__ void classify(const float4& pi, const float4& pj, flo
 // ---------------------------------------------------------------------------------------
 constexpr int kListBatch = 8;
 
+// Offset of slot k's entry 0 in the tiled list array (entry q at + q * kListTile).
+__device__ __forceinline__ size_t list_base(uint32_t k, uint32_t cap) {
+  return (size_t)(k / kListTile) * cap * kListTile + (k % kListTile);
+}
+
 __device__ __forceinline__ void list_push(const SphArgs& a, uint32_t* my, uint32_t& cnt, uint32_t k, int row,
                                           uint32_t t) {
   if (cnt < a.cap) {
-    my[cnt] = t;
+    my[(size_t)cnt * kListTile] = t;
   } else if (cnt == a.cap) {
     a.nresume[2 * (size_t)k] = (uint32_t)row;
     a.nresume[2 * (size_t)k + 1] = t;
@@ -218,7 +223,7 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_kernel(SphArgs a, int
     const float4 pi = PF[T.k];
     const float thr = prefilter_threshold<EXACT_PF>(K, pi);
     const float thr_lo = XD < 0 ? 0.f : certain_threshold(K, pi);
-    uint32_t* __restrict__ my = a.nlist + (size_t)T.k * a.cap;
+    uint32_t* __restrict__ my = a.nlist + list_base(T.k, a.cap);  // entry q at my[q * kListTile]
     uint32_t cnt = 0;
     int row = 0;
     uint32_t t = 0, e = 0;
@@ -292,14 +297,14 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_pass_kernel(SphArgs a
     P.begin(a, K, k);
     const uint32_t cnt = live ? a.nlen[k] : 0u;
     const uint32_t L = min(cnt, cap);
-    const uint32_t* __restrict__ my = a.nlist + (size_t)k * cap;
+    const uint32_t* __restrict__ my = a.nlist + list_base(k, cap);  // entry q at my[q * kListTile]
     if constexpr (PrefetchPolicy<Pairs>::value) {
       // software pipeline: list entries two ahead, the neighbour's pack records one ahead
       uint32_t t = L ? my[0] : k;
-      uint32_t tn = L > 1 ? my[1] : t;
+      uint32_t tn = L > 1 ? my[kListTile] : t;
       typename Pairs::Pre cur = P.fetch(t);
       for (uint32_t q = 0; q < L; ++q) {
-        const uint32_t tnn = q + 2 < L ? my[q + 2] : tn;
+        const uint32_t tnn = q + 2 < L ? my[(q + 2) * kListTile] : tn;
         const typename Pairs::Pre nxt = P.fetch(tn);
         P.pair_with(t, cur);
         cur = nxt;
@@ -307,7 +312,7 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_pass_kernel(SphArgs a
         tn = tnn;
       }
     } else {
-      for (uint32_t q = 0; q < L; ++q) P.pair(my[q]);
+      for (uint32_t q = 0; q < L; ++q) P.pair(my[q * kListTile]);
     }
     if (cnt > cap) {
       // rare: continue the candidate walk where the list stopped
