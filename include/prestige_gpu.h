@@ -122,6 +122,23 @@ int pg_destroy(pg_system* sys);
 int pg_set_field(pg_system* sys, const char* name, const void* host, size_t count, int dtype);
 int pg_get_field(pg_system* sys, const char* name, void* host, size_t count, int dtype);
 
+/* Asynchronous host I/O for step loops that exchange data with the host every step (no
+ * reference counterpart: its slices live in host memory).  Host buffers must stay valid, and
+ * for inputs unchanged, until pg_wait_io returns; page-locked (pinned) buffers let the copies
+ * overlap the steps.  Only fields that exist, in their own precision (dtype = the system's for
+ * pos/vel/rho/mass/acc/drho, PG_F64 for user fields).
+ *   pg_set_field_async  copies `host` into a staging buffer on an input copy stream; every later
+ *                       call on the handle (a step, a rates or neighbour call, a field read)
+ *                       first moves it into the field.  So inputs for step k+1 upload while
+ *                       step k runs.
+ *   pg_get_field_async  snapshots the field at this point of the handle's work (a device copy)
+ *                       and copies the snapshot to `host` on an output copy stream; later steps
+ *                       do not disturb it.  So results of step k download while step k+1 runs.
+ *   pg_wait_io          waits for every copy and step of the handle and reports errors. */
+int pg_set_field_async(pg_system* sys, const char* name, const void* host, size_t count, int dtype);
+int pg_get_field_async(pg_system* sys, const char* name, void* host, size_t count, int dtype);
+int pg_wait_io(pg_system* sys);
+
 /* Neighbour search: cell hash, stable (cell, id) sort, cell-start table.  Replaces the all-pairs
  * `for j in 0..n` of prestige/src/codegen/simple_cpu.rs:8. */
 int pg_build_neighbors(pg_system* sys);

@@ -68,6 +68,9 @@ SIGNATURES = {
     "pg_destroy": (_I, [_P]),
     "pg_set_field": (_I, [_P, _S, _P, _SZ, _I]),
     "pg_get_field": (_I, [_P, _S, _P, _SZ, _I]),
+    "pg_set_field_async": (_I, [_P, _S, _P, _SZ, _I]),
+    "pg_get_field_async": (_I, [_P, _S, _P, _SZ, _I]),
+    "pg_wait_io": (_I, [_P]),
     "pg_build_neighbors": (_I, [_P]),
     "pg_num_cells": (_I, [_P, ctypes.POINTER(_SZ)]),
     "pg_get_neighbors": (_I, [_P, _P, _P, _P, _SZ]),

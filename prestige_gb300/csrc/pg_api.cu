@@ -583,9 +583,54 @@ DevBuf* find_field(pg_system* s, const char* name, int* comps, bool* sys_prec, b
   return nullptr;
 }
 
+int io_streams(pg_system* s) {
+  if (!s->io_in) PG_CUDA_TRY(cudaStreamCreateWithFlags(&s->io_in, cudaStreamNonBlocking));
+  if (!s->io_out) PG_CUDA_TRY(cudaStreamCreateWithFlags(&s->io_out, cudaStreamNonBlocking));
+  return PG_OK;
+}
+
+int io_slot(pg_system* s, const std::string& name, pg_system::IoSlot** out) {
+  PG_TRY(io_streams(s));
+  pg_system::IoSlot& sl = s->io[name];
+  if (!sl.in_ready) {
+    for (cudaEvent_t* e : {&sl.in_ready, &sl.in_free, &sl.snap_ready, &sl.snap_free})
+      PG_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    PG_CUDA_TRY(cudaEventRecord(sl.in_free, s->stream));
+    PG_CUDA_TRY(cudaEventRecord(sl.snap_free, s->io_out));
+  }
+  *out = &sl;
+  return PG_OK;
+}
+
+// Moves the inputs staged by pg_set_field_async into their fields, on the compute stream, before
+// any later work of the handle.
+int apply_io_inputs(pg_system* s) {
+  for (auto& kv : s->io) {
+    pg_system::IoSlot& sl = kv.second;
+    if (!sl.pending) continue;
+    int comps;
+    bool sys_prec, writable;
+    DevBuf* b = find_field(s, kv.first.c_str(), &comps, &sys_prec, &writable);
+    sl.pending = false;
+    if (!b) continue;
+    PG_CUDA_TRY(cudaStreamWaitEvent(s->stream, sl.in_ready, 0));
+    if (sl.in_bytes) PG_CUDA_TRY(cudaMemcpyAsync(b->p, sl.stage.p, sl.in_bytes, cudaMemcpyDeviceToDevice, s->stream));
+    PG_CUDA_TRY(cudaEventRecord(sl.in_free, s->stream));
+    s->nbr_valid = false;
+  }
+  return PG_OK;
+}
+
 }  // namespace pg
 
 pg_system::~pg_system() {
+  if (io_in) cudaStreamSynchronize(io_in);
+  if (io_out) cudaStreamSynchronize(io_out);
+  for (auto& kv : io)
+    for (cudaEvent_t e : {kv.second.in_ready, kv.second.in_free, kv.second.snap_ready, kv.second.snap_free})
+      if (e) cudaEventDestroy(e);
+  if (io_in) cudaStreamDestroy(io_in);
+  if (io_out) cudaStreamDestroy(io_out);
   drop_graphs(this);
   for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
   for (cudaEvent_t e : ev_pending) cudaEventDestroy(e);
@@ -709,12 +754,46 @@ int pg_destroy(pg_system* s) {
   return PG_OK;
 }
 
+// Every entry point starts here: inputs staged by pg_set_field_async take effect before the call.
 static int check(pg_system* s) {
   pg::clear_error();
   if (!s) {
     pg::set_error("null handle");
     return PG_EINVAL;
   }
+  return s->io.empty() ? PG_OK : pg::apply_io_inputs(s);
+}
+
+// Field, element count and byte size for the asynchronous copies (system precision only).
+static int io_field(pg_system* s, const char* name, const void* host, size_t count, int dtype, bool input,
+                    pg::DevBuf** out, size_t* bytes) {
+  if (!name || (!host && count)) {
+    pg::set_error("null name or buffer");
+    return PG_EINVAL;
+  }
+  int comps;
+  bool sys_prec, writable;
+  pg::DevBuf* b = pg::find_field(s, name, &comps, &sys_prec, &writable);
+  if (!b) {
+    pg::set_error("unknown field '%s' (asynchronous copies need an existing field)", name);
+    return PG_ENOTFOUND;
+  }
+  if (input && !writable) {
+    pg::set_error("field '%s' is read-only", name);
+    return PG_EINVAL;
+  }
+  if (count != s->n * (size_t)comps) {
+    pg::set_error("field '%s' has %zu values (got %zu)", name, s->n * (size_t)comps, count);
+    return PG_EINVAL;
+  }
+  int have = sys_prec ? (s->f64 ? PG_F64 : PG_F32) : PG_F64;
+  if (std::string(name) == "acc" || std::string(name) == "drho") have = s->f64 ? PG_F64 : PG_F32;
+  if (dtype != have) {
+    pg::set_error("asynchronous copies of '%s' need its own precision (dtype %d)", name, have);
+    return PG_EINVAL;
+  }
+  *out = b;
+  *bytes = (have == PG_F64 ? 8 : 4) * count;
   return PG_OK;
 }
 
@@ -768,6 +847,48 @@ int pg_set_field(pg_system* s, const char* name, const void* host, size_t count,
   PG_CUDA_TRY(cudaStreamSynchronize(s->stream));
   s->nbr_valid = false;
   return PG_OK;
+}
+
+int pg_set_field_async(pg_system* s, const char* name, const void* host, size_t count, int dtype) {
+  PG_TRY(check(s));
+  pg::DevBuf* b;
+  size_t bytes;
+  PG_TRY(io_field(s, name, host, count, dtype, true, &b, &bytes));
+  pg_system::IoSlot* sl;
+  PG_TRY(pg::io_slot(s, name, &sl));
+  PG_TRY(sl->stage.ensure(bytes ? bytes : 8));
+  PG_CUDA_TRY(cudaStreamWaitEvent(s->io_in, sl->in_free, 0));
+  if (bytes) PG_CUDA_TRY(cudaMemcpyAsync(sl->stage.p, host, bytes, cudaMemcpyHostToDevice, s->io_in));
+  PG_CUDA_TRY(cudaEventRecord(sl->in_ready, s->io_in));
+  sl->in_bytes = bytes;
+  sl->pending = true;
+  s->nbr_valid = false;
+  return PG_OK;
+}
+
+int pg_get_field_async(pg_system* s, const char* name, void* host, size_t count, int dtype) {
+  PG_TRY(check(s));
+  pg::DevBuf* b;
+  size_t bytes;
+  PG_TRY(io_field(s, name, host, count, dtype, false, &b, &bytes));
+  pg_system::IoSlot* sl;
+  PG_TRY(pg::io_slot(s, name, &sl));
+  PG_TRY(sl->snap.ensure(bytes ? bytes : 8));
+  // the snapshot is taken at this point of the compute stream, once its previous copy-out is done
+  PG_CUDA_TRY(cudaStreamWaitEvent(s->stream, sl->snap_free, 0));
+  if (bytes) PG_CUDA_TRY(cudaMemcpyAsync(sl->snap.p, b->p, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  PG_CUDA_TRY(cudaEventRecord(sl->snap_ready, s->stream));
+  PG_CUDA_TRY(cudaStreamWaitEvent(s->io_out, sl->snap_ready, 0));
+  if (bytes) PG_CUDA_TRY(cudaMemcpyAsync(host, sl->snap.p, bytes, cudaMemcpyDeviceToHost, s->io_out));
+  PG_CUDA_TRY(cudaEventRecord(sl->snap_free, s->io_out));
+  return PG_OK;
+}
+
+int pg_wait_io(pg_system* s) {
+  PG_TRY(check(s));
+  if (s->io_in) PG_CUDA_TRY(cudaStreamSynchronize(s->io_in));
+  if (s->io_out) PG_CUDA_TRY(cudaStreamSynchronize(s->io_out));
+  return pg::sync_and_check(s);
 }
 
 int pg_get_field(pg_system* s, const char* name, void* host, size_t count, int dtype) {

@@ -61,6 +61,17 @@ struct pg_system {
   // device error word
   pg::DevBuf err;
 
+  // asynchronous host I/O (pg_set_field_async / pg_get_field_async): per field a staging buffer
+  // for inputs and a snapshot buffer for outputs, one copy stream per direction
+  struct IoSlot {
+    pg::DevBuf stage, snap;
+    size_t in_bytes = 0;
+    bool pending = false;  // staged input not yet moved into the field
+    cudaEvent_t in_ready = nullptr, in_free = nullptr, snap_ready = nullptr, snap_free = nullptr;
+  };
+  std::map<std::string, IoSlot> io;
+  cudaStream_t io_in = nullptr, io_out = nullptr;
+
   // CUDA graph of one step (DEM: one per history parity)
   bool graph_enabled = false;
   int list_arith = -1;  // arithmetic mode of the pair lists in nlist/nlen (-1: none built yet)
@@ -91,6 +102,7 @@ int sync_and_check(pg_system* s);
 int choose_pass_grid(pg_system* s);
 int retune_sph(pg_system* s, double mult, int f64_mode, int block);
 int enqueue_step(pg_system* s);
+int apply_io_inputs(pg_system* s);
 void drop_graphs(pg_system* s);
 int capture_graphs(pg_system* s);
 void destroy_adjoint(pg_system* s);

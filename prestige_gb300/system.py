@@ -132,6 +132,21 @@ class ParticleSystem:
         nat.check(self._lib.pg_get_field(self._h, name.encode(), ptr, count, nat.PG_F64 if f64 else nat.PG_F32),
                   "pg_get_field")
 
+    def set_ptr_async(self, name, ptr, count, f64=True):
+        """Stage a copy from a raw (pinned) host pointer; it takes effect before the next call on
+        this handle.  The buffer must stay unchanged until wait_io()."""
+        nat.check(self._lib.pg_set_field_async(self._h, name.encode(), ptr, count,
+                                               nat.PG_F64 if f64 else nat.PG_F32), "pg_set_field_async")
+
+    def get_ptr_async(self, name, ptr, count, f64=True):
+        """Snapshot the named slice now and copy it to a raw (pinned) host pointer in the
+        background; the data is there after wait_io()."""
+        nat.check(self._lib.pg_get_field_async(self._h, name.encode(), ptr, count,
+                                               nat.PG_F64 if f64 else nat.PG_F32), "pg_get_field_async")
+
+    def wait_io(self):
+        nat.check(self._lib.pg_wait_io(self._h), "pg_wait_io")
+
     # -- neighbour search -----------------------------------------------------------------------
     def num_cells(self):
         v = ctypes.c_size_t()
