@@ -138,6 +138,10 @@ int ensure_sorted_buffers(pg_system* s) {
   PG_TRY(s->nlist.ensure(4 * ((n + kListTile - 1) / kListTile) * kListTile * (size_t)s->list_cap));
   PG_TRY(s->nlen.ensure(4 * n));
   PG_TRY(s->nresume.ensure(8 * n));
+  PG_TRY(s->posmin.ensure(3 * sizeof(unsigned long long)));
+  double hmax = 0.0;
+  for (const pg_config& c : s->cfgs) hmax = std::max(hmax, c.h);
+  s->pos_pad = 8.0 * hmax;
   return PG_OK;
 }
 
@@ -166,6 +170,8 @@ SphArgs sph_args(pg_system* s, int integrate, bool rates) {
   a.nresume = s->nresume.as<uint32_t>();
   a.cap = (uint32_t)s->list_cap;
   a.err = s->err.as<unsigned>();
+  a.posmin = s->posmin.as<unsigned long long>();
+  a.pos_pad = s->pos_pad;
   return a;
 }
 
@@ -188,8 +194,14 @@ NbrArgs nbr_args(pg_system* s) {
 // Hash + stable sort + cell table for the current positions (enqueued on the stream).
 int enqueue_neighbors(pg_system* s) {
   const void* pos = s->pos.p;
+  // the double-word packs need the step's minimum position (sph_gather_df)
+  unsigned long long* posmin = nullptr;
+  if (s->model == PG_MODEL_SPH && s->arith == ARITH_F64_DF && s->posmin.p) {
+    posmin = s->posmin.as<unsigned long long>();
+    PG_CUDA_TRY(cudaMemsetAsync(posmin, 0xff, 3 * sizeof(unsigned long long), s->stream));
+  }
   PG_TRY(launch_hash(s->stream, s->gridk.as<GridK>(), s->nsys > 1 ? s->sys_of_id.as<uint32_t>() : nullptr, s->f64,
-                     s->dim, pos, s->n, s->nw.keys[0].as<uint32_t>(), s->nw.vals[0].as<uint32_t>()));
+                     s->dim, pos, s->n, s->nw.keys[0].as<uint32_t>(), s->nw.vals[0].as<uint32_t>(), posmin));
   PG_TRY(sort_and_table(s->stream, s->nw));
   return PG_OK;
 }

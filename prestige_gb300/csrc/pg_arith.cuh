@@ -12,6 +12,7 @@
 //   TwoSum            Knuth, TAOCP vol. 2 (6 operations, error-free)
 //   Fast2Sum          Dekker 1971 (3 operations, error-free when |a| >= |b|)
 //   TwoProd           with a fused multiply-add (2 operations, error-free)
+//   df_sub_close      x - y for operands whose hi parts are within a factor 2 (Sterbenz)
 //   df_add            "SloppyDWPlusDW" (Dekker 1971; Joldes, Muller & Popescu 2017, Alg. 5):
 //                     absolute error <= ~2u^2 (|x| + |y|), u = 2^-24, which is what a sum of
 //                     pair terms needs (errors relative to the sum of magnitudes)
@@ -114,6 +115,13 @@ __device__ __forceinline__ df df_add(df x, df y) {
 }
 
 __device__ __forceinline__ df df_sub(df x, df y) { return df_add(x, df_neg(y)); }
+
+// x - y when the hi parts lie within a factor 2 of each other, so that their difference is exact
+// (Sterbenz 1974): 5 operations in place of 11.  Fast2Sum applies because a nonzero hi
+// difference is at least one ulp of the operands and each lo part is at most half of one.
+__device__ __forceinline__ df df_sub_close(df x, df y) {
+  return fast_two_sum(__fsub_rn(x.hi, y.hi), __fsub_rn(x.lo, y.lo));
+}
 
 __device__ __forceinline__ df df_add_f(df x, float y) {
   const df s = two_sum(x.hi, y);

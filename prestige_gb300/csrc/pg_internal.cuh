@@ -114,8 +114,19 @@ struct NbrWork {
 };
 
 // Cell key and id of every particle (id order) into w.keys[0] / w.vals[0].
+// posmin (optional, f64 positions only): per-dimension minimum position, as ordered_code values,
+// folded in with atomicMin (the caller presets it to all ones).
 int launch_hash(cudaStream_t st, const GridK* grid_dev, const uint32_t* sys_of_id, int f64, int dim,
-                const void* pos, size_t n, uint32_t* keys, uint32_t* vals);
+                const void* pos, size_t n, uint32_t* keys, uint32_t* vals, unsigned long long* posmin = nullptr);
+
+// Order-preserving map of doubles to unsigned 64-bit integers (and back), for atomicMin.
+__device__ __forceinline__ unsigned long long ordered_code(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ordered_value(unsigned long long u) {
+  return __longlong_as_double((long long)((u >> 63) ? (u & 0x7fffffffffffffffull) : ~u));
+}
 // Sort (cell, id) pairs already in keys[0]/vals[0] and build cell_start.
 int sort_and_table(cudaStream_t st, NbrWork& w);
 // Exclusive scan of m u32 values into out[0..m] (out[m] = total).  tmp: scan_tmp_words(m).

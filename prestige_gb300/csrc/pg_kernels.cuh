@@ -67,6 +67,9 @@ struct SphArgs {
   void* mass;
   void* acc;                 // optional rates output, id order
   void* drho;
+  unsigned long long* posmin;  // double-word mode: per-dimension minimum position of the step,
+                               // order-preserving integer code (pos_min_kernel)
+  double pos_pad;              // double-word mode: packed positions are x - min + pos_pad (>= 8h)
   void* lam[5];              // adjoint (pg_adjoint.cu): lambda_x, lambda_v, lambda_rho, dL/dalpha and
                              // dL/dB partial sums, all id order
   uint32_t* nlist;           // neighbour lists in tiles of kListTile slots: entry q of slot k at

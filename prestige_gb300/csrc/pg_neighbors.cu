@@ -130,23 +130,43 @@ __device__ __forceinline__ int cell_coord_f(float x, float lo, float inv, int n)
   return (int)t;
 }
 
-template <class R, int DIM>
+// Cell key and id of every particle.  MIN: also the per-dimension minimum position (block
+// reduction, one atomicMin per block and dimension; blockDim.x == 256).
+template <class R, int DIM, bool MIN>
 __global__ void hash_kernel(const GridK* __restrict__ grid, const uint32_t* __restrict__ sys_of_id,
                             const R* __restrict__ pos, uint32_t n, uint32_t* __restrict__ keys,
-                            uint32_t* __restrict__ vals) {
+                            uint32_t* __restrict__ vals, unsigned long long* __restrict__ posmin) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const GridK& g = grid[sys_of_id ? sys_of_id[i] : 0u];
-  int c[3] = {0, 0, 0};
-  const int nn[3] = {g.nx, g.ny, g.nz};
+  unsigned long long m[3] = {~0ull, ~0ull, ~0ull};
+  if (i < n) {
+    const GridK& g = grid[sys_of_id ? sys_of_id[i] : 0u];
+    int c[3] = {0, 0, 0};
+    const int nn[3] = {g.nx, g.ny, g.nz};
 #pragma unroll
-  for (int d = 0; d < DIM; ++d) {
-    const R x = pos[(size_t)i * DIM + d];
-    if (sizeof(R) == 8) c[d] = cell_coord_d((double)x, g.lo[d], g.inv, nn[d]);
-    else c[d] = cell_coord_f((float)x, g.lof[d], g.invf, nn[d]);
+    for (int d = 0; d < DIM; ++d) {
+      const R x = pos[(size_t)i * DIM + d];
+      if (sizeof(R) == 8) c[d] = cell_coord_d((double)x, g.lo[d], g.inv, nn[d]);
+      else c[d] = cell_coord_f((float)x, g.lof[d], g.invf, nn[d]);
+      if (MIN) m[d] = ordered_code((double)x);
+    }
+    keys[i] = g.cell_base + ((uint32_t)c[2] * (uint32_t)g.ny + (uint32_t)c[1]) * (uint32_t)g.nx + (uint32_t)c[0];
+    vals[i] = i;
   }
-  keys[i] = g.cell_base + ((uint32_t)c[2] * (uint32_t)g.ny + (uint32_t)c[1]) * (uint32_t)g.nx + (uint32_t)c[0];
-  vals[i] = i;
+  if (MIN) {
+    __shared__ unsigned long long part[DIM][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      for (int o = 16; o; o >>= 1) m[d] = min(m[d], __shfl_down_sync(0xffffffffu, m[d], o));
+      if (lane == 0) part[d][warp] = m[d];
+    }
+    __syncthreads();
+    if (threadIdx.x < DIM) {
+      unsigned long long v = part[threadIdx.x][0];
+      for (int w = 1; w < 8; ++w) v = min(v, part[threadIdx.x][w]);
+      atomicMin(posmin + threadIdx.x, v);
+    }
+  }
 }
 
 template <class R, int DIM>
@@ -276,15 +296,19 @@ inline unsigned blocks_for(size_t n, int t) { return (unsigned)((n + t - 1) / t)
 }  // namespace
 
 int launch_hash(cudaStream_t st, const GridK* grid_dev, const uint32_t* sys_of_id, int f64, int dim, const void* pos,
-                size_t n, uint32_t* keys, uint32_t* vals) {
+                size_t n, uint32_t* keys, uint32_t* vals, unsigned long long* posmin) {
   if (n == 0) return PG_OK;
   const unsigned b = blocks_for(n, 256);
-  if (f64) {
-    if (dim == 2) hash_kernel<double, 2><<<b, 256, 0, st>>>(grid_dev, sys_of_id, (const double*)pos, (uint32_t)n, keys, vals);
-    else hash_kernel<double, 3><<<b, 256, 0, st>>>(grid_dev, sys_of_id, (const double*)pos, (uint32_t)n, keys, vals);
+  const uint32_t m = (uint32_t)n;
+  if (f64 && posmin) {
+    if (dim == 2) hash_kernel<double, 2, true><<<b, 256, 0, st>>>(grid_dev, sys_of_id, (const double*)pos, m, keys, vals, posmin);
+    else hash_kernel<double, 3, true><<<b, 256, 0, st>>>(grid_dev, sys_of_id, (const double*)pos, m, keys, vals, posmin);
+  } else if (f64) {
+    if (dim == 2) hash_kernel<double, 2, false><<<b, 256, 0, st>>>(grid_dev, sys_of_id, (const double*)pos, m, keys, vals, nullptr);
+    else hash_kernel<double, 3, false><<<b, 256, 0, st>>>(grid_dev, sys_of_id, (const double*)pos, m, keys, vals, nullptr);
   } else {
-    if (dim == 2) hash_kernel<float, 2><<<b, 256, 0, st>>>(grid_dev, sys_of_id, (const float*)pos, (uint32_t)n, keys, vals);
-    else hash_kernel<float, 3><<<b, 256, 0, st>>>(grid_dev, sys_of_id, (const float*)pos, (uint32_t)n, keys, vals);
+    if (dim == 2) hash_kernel<float, 2, false><<<b, 256, 0, st>>>(grid_dev, sys_of_id, (const float*)pos, m, keys, vals, nullptr);
+    else hash_kernel<float, 3, false><<<b, 256, 0, st>>>(grid_dev, sys_of_id, (const float*)pos, m, keys, vals, nullptr);
   }
   PG_CUDA_TRY(cudaGetLastError());
   return PG_OK;

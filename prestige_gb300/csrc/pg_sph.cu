@@ -94,6 +94,12 @@ struct __align__(64) DfRecord {
   float4 ah, al, bh, bl;
 };
 
+// Packs of the double-word mode.  Positions in the record and in the FP32 array are shifted by
+// pos_pad - min (per dimension), so every packed coordinate is at least 8h: the hi parts of two
+// particles closer than 2h are then within a factor 2 of each other and the pair passes take
+// differences with df_sub_close.  The shift is common to all particles, so differences are
+// unchanged up to one f64 rounding of each shifted coordinate; the f64 array for the exact test
+// keeps the unshifted positions.
 template <int DIM>
 __global__ void sph_gather_df(SphArgs a) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -110,10 +116,13 @@ __global__ void sph_gather_df(SphArgs a) {
     x[c] = pos[(size_t)id * DIM + c];
     v[c] = vel[(size_t)id * DIM + c];
   }
+  double xs[3] = {a.pos_pad, a.pos_pad, a.pos_pad};
+#pragma unroll
+  for (int c = 0; c < DIM; ++c) xs[c] = __dadd_rn(__dsub_rn(x[c], ordered_value(a.posmin[c])), a.pos_pad);
   float4 ah, al, bh, bl;
-  df_split(x[0], &ah.x, &al.x);
-  df_split(x[1], &ah.y, &al.y);
-  df_split(x[2], &ah.z, &al.z);
+  df_split(xs[0], &ah.x, &al.x);
+  df_split(xs[1], &ah.y, &al.y);
+  df_split(xs[2], &ah.z, &al.z);
   df_split(m, &ah.w, &al.w);
   df_split(v[0], &bh.x, &bl.x);
   df_split(v[1], &bh.y, &bl.y);
@@ -284,9 +293,9 @@ struct DfPairs {
   template <bool CHECK>
   __device__ __forceinline__ bool geometry(uint32_t t, const Pre& p, df* d, df& r2, df& F, df& wv, df& mj) const {
     const float4 ah = p.ah, al = p.al;
-    d[0] = df_sub(xi[0], df_make(ah.x, al.x));
-    d[1] = df_sub(xi[1], df_make(ah.y, al.y));
-    d[2] = DIM == 3 ? df_sub(xi[2], df_make(ah.z, al.z)) : df_make(0.f, 0.f);
+    d[0] = df_sub_close(xi[0], df_make(ah.x, al.x));
+    d[1] = df_sub_close(xi[1], df_make(ah.y, al.y));
+    d[2] = DIM == 3 ? df_sub_close(xi[2], df_make(ah.z, al.z)) : df_make(0.f, 0.f);
     r2 = df_sumsq3(d[0], d[1], d[2]);
     if (CHECK) {
       const df gap = df_sub(r2, df_make(w.four_h2[0], w.four_h2[1]));
@@ -463,7 +472,7 @@ int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith) {
       if (dim == 2) sph_gather_real<OpsD, 2><<<blocks, 256, 0, st>>>(a);
       else sph_gather_real<OpsD, 3><<<blocks, 256, 0, st>>>(a);
       break;
-    case ARITH_F64_DF:
+    case ARITH_F64_DF:  // a.posmin was filled by the step's hash kernel
       if (dim == 2) sph_gather_df<2><<<blocks, 256, 0, st>>>(a);
       else sph_gather_df<3><<<blocks, 256, 0, st>>>(a);
       break;

@@ -52,6 +52,8 @@ struct pg_system {
   int block = 128;               // threads per block of the list-based SPH kernels
   int list_cap = 128;            // neighbour-list slots per particle
   pg::DevBuf nlist, nlen, nresume;
+  pg::DevBuf posmin;             // 3 x u64, double-word mode (pos_min_kernel)
+  double pos_pad = 0.0;          // 8 x the largest h of the handle's systems
 
   // DEM contact history, id order, double buffered
   pg::DevBuf hpid[2], hxi[2];

@@ -84,7 +84,16 @@ class System {
   void set(const std::string& name, const std::vector<double>& values);
   std::vector<double> get(const std::string& name) const;
 
+  // Asynchronous host I/O for step loops (f64 handles): set_async stages `values` (which must
+  // stay valid and unchanged until wait_io) and the next call on the handle moves it into the
+  // slice; get_async snapshots the slice now and fills `out` by wait_io.  Pinned host memory lets
+  // the copies overlap the steps.
+  void set_async(const std::string& name, const double* values, size_t count);
+  void get_async(const std::string& name, double* out, size_t count);
+  void wait_io();
+
   void step(int nsteps = 1);
+  void step_async(int nsteps = 1);
   void compute_rates();
   void gather_sum(const std::string& dst, const std::string& src);
   void run_equations(const std::vector<std::string>& bodies);

@@ -217,7 +217,19 @@ std::vector<double> System::get(const std::string& name) const {
   return out;
 }
 
+void System::set_async(const std::string& name, const double* values, size_t count) {
+  check(pg_set_field_async(h_, name.c_str(), values, count, PG_F64), "pg_set_field_async");
+}
+
+void System::get_async(const std::string& name, double* out, size_t count) {
+  check(pg_get_field_async(h_, name.c_str(), out, count, PG_F64), "pg_get_field_async");
+}
+
+void System::wait_io() { check(pg_wait_io(h_), "pg_wait_io"); }
+
 void System::step(int nsteps) { check(pg_step(h_, nsteps), "pg_step"); }
+
+void System::step_async(int nsteps) { check(pg_step_async(h_, nsteps), "pg_step_async"); }
 
 void System::compute_rates() { check(pg_compute_rates(h_), "pg_compute_rates"); }
 

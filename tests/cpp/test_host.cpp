@@ -186,6 +186,36 @@ static void test_gpu_step_and_adjoint() {
   CHECK(threw);
 }
 
+static void test_gpu_async_io() {
+  const int side = 10, n = side * side * side, dim = 3;
+  const double dx = 0.01;
+  std::vector<double> pos(n * dim), vel(n * dim, 0.0), rho(n, 1000.0), mass(n, 1000.0 * dx * dx * dx);
+  for (int i = 0; i < n; ++i) {
+    pos[3 * i] = (i % side + 0.5) * dx;
+    pos[3 * i + 1] = ((i / side) % side + 0.5) * dx;
+    pos[3 * i + 2] = (i / (side * side) + 0.5) * dx;
+    vel[3 * i + 1] = 0.02 * std::cos(30.0 * pos[3 * i]);
+  }
+  pg_config c = sph_config(dim, 1.3 * dx, -0.05, 0.15);
+  c.dt = 0.25 * c.h / c.c0;
+  System a(c, n), b(c, n);
+  for (System* s : {&a, &b}) {
+    s->set("pos", pos);
+    s->set("vel", vel);
+    s->set("rho", rho);
+    s->set("mass", mass);
+  }
+  a.step(2);
+  std::vector<double> out_pos(pos.size()), out_rho(rho.size());
+  b.set_async("vel", vel.data(), vel.size());
+  b.step_async(2);
+  b.get_async("pos", out_pos.data(), out_pos.size());
+  b.get_async("rho", out_rho.data(), out_rho.size());
+  b.wait_io();
+  CHECK(out_pos == a.get("pos"));
+  CHECK(out_rho == a.get("rho"));
+}
+
 int main(int argc, char** argv) {
   const std::string what = argc > 1 ? argv[1] : "cpu";
   if (what == "cpu") {
@@ -197,6 +227,7 @@ int main(int argc, char** argv) {
     test_gpu_eq1_bit_exact();
     test_gpu_compiled_equations();
     test_gpu_step_and_adjoint();
+    test_gpu_async_io();
   } else {
     std::fprintf(stderr, "usage: test_host cpu|gpu\n");
     return 2;
