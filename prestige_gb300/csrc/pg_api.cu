@@ -75,6 +75,8 @@ SphK make_sphk(const pg_config& c, const Grid& g, uint32_t cell_base, uint32_t i
   df_split(k.d.four_h2, &k.w.four_h2[0], &k.w.four_h2[1]);
   df_split(k.d.avk, &k.w.avk[0], &k.w.avk[1]);
   df_split(k.d.eps_h2, &k.w.eps_h2[0], &k.w.eps_h2[1]);
+  df_split(k.d.B, &k.w.B[0], &k.w.B[1]);
+  df_split(k.d.inv_rho0, &k.w.inv_rho0[0], &k.w.inv_rho0[1]);
   k.w.band = (float)(1e-9 * k.d.four_h2);
   k.two_h_f = (float)(2.0 * h) * 1.0000001f;
   k.id_begin = id_begin;

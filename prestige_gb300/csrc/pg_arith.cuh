@@ -82,6 +82,32 @@ __host__ __device__ __forceinline__ void df_split(double x, float* hi, float* lo
   *lo = (float)(x - (double)h);
 }
 
+// hi = RN32(x), lo = RN32(x - hi) with integer operations only (GB300 issues FP64 and its
+// conversions at 1/64 of the FP32 rate).  The binary64 significand is rounded to 24 bits
+// (nearest, ties to even) and the exact remainder, an integer of at most 30 bits times
+// 2^(e-52), is converted with one integer-to-float rounding and scaled by a power of two.
+// Exponents outside [-70, 126], zeros, infinities and NaNs take the hardware conversions.
+__device__ __forceinline__ void df_split_fast(double x, float* hi, float* lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  if (e < -70 || e > 126) {
+    df_split(x, hi, lo);
+    return;
+  }
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  const unsigned long long mant = b & 0xfffffffffffffull;
+  const unsigned m23 = (unsigned)(mant >> 29);
+  const unsigned rest = (unsigned)(mant & 0x1fffffffu);
+  const unsigned up = (rest > 0x10000000u || (rest == 0x10000000u && (m23 & 1u))) ? 1u : 0u;
+  // hi: carry of the rounding into the exponent is handled by the integer addition
+  const unsigned hbits = (((unsigned)(e + 127) << 23) | m23) + up;
+  *hi = __uint_as_float(sign | hbits);
+  // remainder in units of 2^(e-52): rest - up * 2^29, in [-2^28, 2^28]
+  const int r = (int)rest - (int)(up << 29);
+  const float scale = __uint_as_float((unsigned)(e - 52 + 127) << 23);
+  *lo = __uint_as_float(__float_as_uint(__int2float_rn(r) * scale) ^ sign);
+}
+
 __device__ __forceinline__ df df_from_double(double x) {
   const float h = __double2float_rn(x);
   return df_make(h, __double2float_rn(__dsub_rn(x, (double)h)));

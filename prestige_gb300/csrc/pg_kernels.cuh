@@ -37,7 +37,7 @@ struct SphC {
 
 // Double-word (hi, lo) copies of the constants for the f64 fast mode.
 struct SphDF {
-  float fa[2], fb[2], inv_h[2], four_h2[2], avk[2], eps_h2[2];
+  float fa[2], fb[2], inv_h[2], four_h2[2], avk[2], eps_h2[2], B[2], inv_rho0[2];
   float band;  // |r^2 - (2h)^2| below which the exact f64 test decides
 };
 

@@ -81,10 +81,24 @@ __global__ void sph_gather_real(SphArgs a) {
 // Double-word copies for the f64 fast mode:
 //   s0 {x,y,z,m}.hi  s1 {x,y,z,m}.lo  s2 {vx,vy,vz,0}.hi  s3 {vx,vy,vz,0}.lo
 //   s4 {rho.hi, rho.lo, P.hi, P.lo}   s5 double {x,y,z} for the exact neighbour test near the cut-off.
-__device__ __forceinline__ float4 df_pack_rho_p(double rho, double P) {
+// p / rho^2 of the Tait law in double-word arithmetic on the FP32 pipe (relative error about
+// 1e-12: (rho/rho0)^gamma - 1 loses the digits its cancellation takes).
+__device__ __forceinline__ df tait_pterm_df(const SphDF& w, int gamma, df rho) {
+  const df rr = df_mul(rho, df_make(w.inv_rho0[0], w.inv_rho0[1]));
+  df pw = rr;
+  for (int e = 1; e < gamma; ++e) pw = df_mul(pw, rr);
+  const df p = df_mul(df_make(w.B[0], w.B[1]), df_add_f(pw, -1.0f));
+  return df_div(p, df_mul(rho, rho));
+}
+
+// The {rho, P/rho^2} pack of the double-word mode, from the f64 density, without FP64 work
+// beyond the density itself.
+__device__ __forceinline__ float4 df_pack_rho(const SphDF& w, int gamma, double rho) {
   float4 r;
-  df_split(rho, &r.x, &r.y);
-  df_split(P, &r.z, &r.w);
+  df_split_fast(rho, &r.x, &r.y);
+  const df pt = tait_pterm_df(w, gamma, df_make(r.x, r.y));
+  r.z = pt.hi;
+  r.w = pt.lo;
   return r;
 }
 
@@ -120,13 +134,13 @@ __global__ void sph_gather_df(SphArgs a) {
 #pragma unroll
   for (int c = 0; c < DIM; ++c) xs[c] = __dadd_rn(__dsub_rn(x[c], ordered_value(a.posmin[c])), a.pos_pad);
   float4 ah, al, bh, bl;
-  df_split(xs[0], &ah.x, &al.x);
-  df_split(xs[1], &ah.y, &al.y);
-  df_split(xs[2], &ah.z, &al.z);
-  df_split(m, &ah.w, &al.w);
-  df_split(v[0], &bh.x, &bl.x);
-  df_split(v[1], &bh.y, &bl.y);
-  df_split(v[2], &bh.z, &bl.z);
+  df_split_fast(xs[0], &ah.x, &al.x);
+  df_split_fast(xs[1], &ah.y, &al.y);
+  df_split_fast(xs[2], &ah.z, &al.z);
+  df_split_fast(m, &ah.w, &al.w);
+  df_split_fast(v[0], &bh.x, &bl.x);
+  df_split_fast(v[1], &bh.y, &bl.y);
+  df_split_fast(v[2], &bh.z, &bl.z);
   bh.w = bl.w = 0.f;
   ((float4*)a.s[0])[k] = ah;
   DfRecord rec;
@@ -135,7 +149,7 @@ __global__ void sph_gather_df(SphArgs a) {
   rec.bh = bh;
   rec.bl = bl;
   ((DfRecord*)a.s[1])[k] = rec;
-  ((float4*)a.s[4])[k] = df_pack_rho_p(rho, tait_pterm<OpsD>(K.d, K.gamma, rho));
+  ((float4*)a.s[4])[k] = df_pack_rho(K.w, K.gamma, rho);
   ((double4_32a*)a.s[5])[k] = make_double4_32a(x[0], x[1], x[2], 0.0);
 }
 
@@ -359,7 +373,7 @@ struct DfPairs {
       double* rho = (double*)a.rho;
       const double rn = __dadd_rn(rho[id], __dmul_rn(c.dt, dfacc_to_double(dr)));
       rho[id] = rn;
-      ((float4*)a.s[4])[k] = df_pack_rho_p(rn, tait_pterm<OpsD>(c, K.gamma, rn));
+      ((float4*)a.s[4])[k] = df_pack_rho(K.w, K.gamma, rn);
     } else if (id < K.fluid_end) {
       double* pos = (double*)a.pos;
       double* vel = (double*)a.vel;
