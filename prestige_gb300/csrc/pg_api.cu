@@ -77,6 +77,12 @@ SphK make_sphk(const pg_config& c, const Grid& g, uint32_t cell_base, uint32_t i
   df_split(k.d.eps_h2, &k.w.eps_h2[0], &k.w.eps_h2[1]);
   df_split(k.d.B, &k.w.B[0], &k.w.B[1]);
   df_split(k.d.inv_rho0, &k.w.inv_rho0[0], &k.w.inv_rho0[1]);
+  df_split(-3.0 * fa, &k.w.near0[0], &k.w.near0[1]);
+  df_split(2.25 * fa / h, &k.w.near1[0], &k.w.near1[1]);
+  df_split(-4.0 * fb / h, &k.w.far0[0], &k.w.far0[1]);
+  df_split(fb / (h * h), &k.w.far1[0], &k.w.far1[1]);
+  df_split(4.0 * fb, &k.w.far2[0], &k.w.far2[1]);
+  k.w.h = (float)h;
   k.w.band = (float)(1e-9 * k.d.four_h2);
   k.two_h_f = (float)(2.0 * h) * 1.0000001f;
   k.id_begin = id_begin;

@@ -38,6 +38,11 @@ struct SphC {
 // Double-word (hi, lo) copies of the constants for the f64 fast mode.
 struct SphDF {
   float fa[2], fb[2], inv_h[2], four_h2[2], avk[2], eps_h2[2], B[2], inv_rho0[2];
+  // F = c0 + c1 r + c2 / r, the cubic spline's (dW/dr)/r on each piece: q < 1 (near) and
+  // 1 <= q < 2 (far), with q = r/h:  near c0 = -3 fa, c1 = 2.25 fa/h;  far c0 = -4 fb/h,
+  // c1 = fb/h^2, c2 = 4 fb
+  float near0[2], near1[2], far0[2], far1[2], far2[2];
+  float h;
   float band;  // |r^2 - (2h)^2| below which the exact f64 test decides
 };
 

@@ -322,13 +322,12 @@ struct DfPairs {
     if (!(r2.hi > 0.f)) return false;
     const df inv_r = df_rsqrt(r2);
     const df r = df_mul(r2, inv_r);
-    const df q = df_mul(r, df_make(w.inv_h[0], w.inv_h[1]));
-    if (q.hi < 1.0f) {
-      F = df_mul(df_make(w.fa[0], w.fa[1]), df_add_f(df_mul_f(q, 2.25f), -3.0f));
-    } else {
-      const df tq = df_add_f(df_neg(q), 2.0f);
-      F = df_mul(df_mul(df_make(w.fb[0], w.fb[1]), df_mul(tq, tq)), inv_r);
-    }
+    // F = c0 + c1 r + c2 / r on either piece of the spline, without a branch
+    const bool near = r.hi < w.h;
+    const df c0 = near ? df_make(w.near0[0], w.near0[1]) : df_make(w.far0[0], w.far0[1]);
+    const df c1 = near ? df_make(w.near1[0], w.near1[1]) : df_make(w.far1[0], w.far1[1]);
+    const df c2 = near ? df_make(0.f, 0.f) : df_make(w.far2[0], w.far2[1]);
+    F = df_add(df_add(c0, df_mul(c1, r)), df_mul(c2, inv_r));
     const float4 bh = p.bh, bl = p.bl;
     const df dv0 = df_sub(vi[0], df_make(bh.x, bl.x));
     const df dv1 = df_sub(vi[1], df_make(bh.y, bl.y));
@@ -339,11 +338,11 @@ struct DfPairs {
   }
 
   __device__ __forceinline__ void momentum(const float4& rpj, const df* d, df r2, df F, df wv, df mj) {
-    df pij = df_make(0.f, 0.f);
-    if (wv.hi < 0.f) {
-      const df den = df_mul(df_add(r2, df_make(w.eps_h2[0], w.eps_h2[1])), df_add(rhoi, df_make(rpj.x, rpj.y)));
-      pij = df_div(df_mul(df_make(w.avk[0], w.avk[1]), wv), den);
-    }
+    // artificial viscosity where the pair approaches (w < 0), computed for every pair and then
+    // selected: nearly every warp has lanes on both sides
+    const df den = df_mul(df_add(r2, df_make(w.eps_h2[0], w.eps_h2[1])), df_add(rhoi, df_make(rpj.x, rpj.y)));
+    const df av = df_div(df_mul(df_make(w.avk[0], w.avk[1]), wv), den);
+    const df pij = wv.hi < 0.f ? av : df_make(0.f, 0.f);
     const df ncoef = df_neg(df_mul(mj, df_mul(df_add(df_add(Pi, df_make(rpj.z, rpj.w)), pij), F)));
     dfacc_add_prod(acc[0], ncoef, d[0]);
     dfacc_add_prod(acc[1], ncoef, d[1]);
