@@ -299,10 +299,12 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_pass_kernel(SphArgs a
     const uint32_t L = min(cnt, cap);
     const uint32_t* __restrict__ my = a.nlist + list_base(k, cap);  // entry q at my[q * kListTile]
     if constexpr (PrefetchPolicy<Pairs>::value) {
-      // software pipeline: list entries two ahead, the neighbour's pack records one ahead
+      // software pipeline: list entries two ahead, the neighbour's pack records one ahead; the
+      // unrolled pair bodies (branch-free) interleave
       uint32_t t = L ? my[0] : k;
       uint32_t tn = L > 1 ? my[kListTile] : t;
       typename Pairs::Pre cur = P.fetch(t);
+#pragma unroll 2
       for (uint32_t q = 0; q < L; ++q) {
         const uint32_t tnn = q + 2 < L ? my[(q + 2) * kListTile] : tn;
         const typename Pairs::Pre nxt = P.fetch(tn);
