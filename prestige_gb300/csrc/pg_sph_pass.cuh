@@ -225,17 +225,26 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_kernel(SphArgs a, int
     const float thr_lo = XD < 0 ? 0.f : certain_threshold(K, pi);
     uint32_t* __restrict__ my = a.nlist + list_base(T.k, a.cap);  // entry q at my[q * kListTile]
     uint32_t cnt = 0;
-    int row = 0;
-    uint32_t t = 0, e = 0;
-    while (true) {
-      while (t >= e && row < nrows) {
-        const int dz = row / side - RZ, dy = row % side - R;
-        ++row;
-        const int z = T.cz + dz, y = T.cy + dy;
-        if (!T.live || z < 0 || z >= g.nz || y < 0 || y >= g.ny) continue;
+    // slot range of a row (empty outside the grid); the next row's range is loaded while the
+    // current row is walked
+    auto row_range = [&](int r, uint32_t& a, uint32_t& b) {
+      const int z = T.cz + r / side - RZ, y = T.cy + r % side - R;
+      a = b = 0;
+      if (T.live && z >= 0 && z < g.nz && y >= 0 && y < g.ny) {
         const uint32_t rb = g.cell_base + ((uint32_t)z * g.ny + (uint32_t)y) * g.nx;
-        t = start[rb + T.x0];
-        e = start[rb + T.x1 + 1];
+        a = start[rb + T.x0];
+        b = start[rb + T.x1 + 1];
+      }
+    };
+    int row = -1, nxt = 0;
+    uint32_t t = 0, e = 0, tn, en;
+    row_range(0, tn, en);
+    while (true) {
+      while (t >= e && nxt < nrows) {
+        t = tn;
+        e = en;
+        row = nxt++;
+        if (nxt < nrows) row_range(nxt, tn, en);
       }
       if (t >= e) break;
       // the batch's candidates that belong to the row, the target itself left out (the packs
@@ -261,7 +270,7 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_kernel(SphArgs a, int
           if (exact_neighbor<DIM>(X, T.k, t + b, K.d.four_h2)) hit |= 1u << b;
         }
       }
-      for (; hit; hit &= hit - 1) list_push(a, my, cnt, T.k, row - 1, t + __ffs(hit) - 1);
+      for (; hit; hit &= hit - 1) list_push(a, my, cnt, T.k, row, t + __ffs(hit) - 1);
       t += kListBatch;
     }
     if (T.live) a.nlen[T.k] = cnt;
