@@ -190,8 +190,25 @@ struct RealPairs {
     dr = R(0);
   }
 
-  __device__ __forceinline__ void pair(uint32_t t) {
-    const R4 Aj = A[t];
+  // The neighbour's pack records, loaded ahead of its pair terms.
+  struct Pre {
+    R4 a, b;
+    R2 q;
+  };
+  static constexpr bool kPrefetch = true;
+
+  __device__ __forceinline__ Pre fetch(uint32_t t) const {
+    Pre p;
+    p.a = A[t];
+    p.b = B[t];
+    if (kMom) p.q = Q[t];
+    return p;
+  }
+
+  __device__ __forceinline__ void pair(uint32_t t) { pair_with(t, fetch(t)); }
+
+  __device__ __forceinline__ void pair_with(uint32_t t, const Pre& p) {
+    const R4 Aj = p.a;
     const R d0 = Ops::sub(xi[0], Aj.x), d1 = Ops::sub(xi[1], Aj.y);
     const R d2 = DIM == 3 ? Ops::sub(xi[2], Aj.z) : R(0);
     R r2 = Ops::add(Ops::mul(d0, d0), Ops::mul(d1, d1));
@@ -200,7 +217,7 @@ struct RealPairs {
       if (!(r2 < c.four_h2)) return;
       if (!(r2 > R(0))) return;
     }
-    const R4 Bj = B[t];
+    const R4 Bj = p.b;
     const R r = Ops::sqrt(r2);
     const R q = Ops::mul(r, c.inv_h);
     R F;
@@ -217,7 +234,7 @@ struct RealPairs {
     const R mj = Aj.w;
     if (kCont) dr = Ops::add(dr, Ops::mul(mj, Ops::mul(w, F)));
     if (kMom) {
-      const R2 qj = Q[t];
+      const R2 qj = p.q;
       R pij = R(0);
       if (w < R(0)) pij = Ops::div(Ops::mul(c.avk, w), Ops::mul(Ops::add(r2, c.eps_h2), Ops::add(rhoi, qj.x)));
       const R coef = Ops::mul(mj, Ops::mul(Ops::add(Ops::add(Pi, qj.y), pij), F));
