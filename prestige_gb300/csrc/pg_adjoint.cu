@@ -363,8 +363,33 @@ struct AdjPairsF {
     s = t;
   }
 
-  __device__ __forceinline__ void pair(uint32_t t) {
-    const float4 xj = XH[t], xj2 = XL[t];
+  // The neighbour's records, loaded ahead of its pair terms.
+  struct Pre {
+    float4 xh, xl, vh, vl, q, a;
+    float db;
+  };
+  static constexpr bool kPrefetch = true;
+
+  __device__ __forceinline__ Pre fetch(uint32_t t) const {
+    Pre p;
+    p.xh = XH[t];
+    p.xl = XL[t];
+    p.vh = VH[t];
+    p.vl = VL[t];
+    if (kMom) {
+      p.q = Q[t];
+      p.a = A[t];
+      p.db = 0.f;
+    } else {
+      p.db = DBp[t];
+    }
+    return p;
+  }
+
+  __device__ __forceinline__ void pair(uint32_t t) { pair_with(t, fetch(t)); }
+
+  __device__ __forceinline__ void pair_with(uint32_t t, const Pre& p) {
+    const float4 xj = p.xh, xj2 = p.xl;
     float d[3];
     d[0] = (xh[0] - xj.x) + (xl[0] - xj2.x);
     d[1] = (xh[1] - xj.y) + (xl[1] - xj2.y);
@@ -373,7 +398,7 @@ struct AdjPairsF {
     if (DIM == 3) r2 += d[2] * d[2];
     // at r = 2h the spline's F and dF/dr vanish, so an FP32 cut-off there adds nothing
     if (!(r2 < four_h2) || !(r2 > 0.f)) return;
-    const float4 vj = VH[t], vj2 = VL[t];
+    const float4 vj = p.vh, vj2 = p.vl;
     const float mj = xj.w;
     float inv_r = rsqrtf(r2);
     inv_r = inv_r * fmaf(-0.5f * r2 * inv_r, inv_r, 1.5f);  // one Newton step
@@ -395,7 +420,7 @@ struct AdjPairsF {
     float w = dv[0] * d[0] + dv[1] * d[1];
     if (DIM == 3) w += dv[2] * d[2];
     if (!kMom) {
-      const float D = dbi * mj + DBp[t] * mi;
+      const float D = dbi * mj + p.db * mi;
       const float gw = G * w * D, fd = F * D;
 #pragma unroll
       for (int c = 0; c < DIM; ++c) {
@@ -404,7 +429,7 @@ struct AdjPairsF {
       }
       return;
     }
-    const float4 qj = Q[t], aj = A[t];
+    const float4 qj = p.q, aj = p.a;
     const float rb = rhoi + vj.w;
     const float e = r2 + eps_h2;
     float c1 = 0.f, c1a = 0.f;
