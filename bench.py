@@ -44,7 +44,7 @@ MOM_BYTES = {"f64": 112, "f32": 56}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per particle of one momentum-pass
 # launch, from the ncu capture summarised in profiles/sph_mom_pass_lattice3d.md (1,000,000
 # particles, f64 double-word mode), scaled by the particle count.
-MOM_TRAFFIC_PER_PARTICLE = {"f64-fast": 508.0}
+MOM_TRAFFIC_PER_PARTICLE = {"f64-fast": 511.0}
 
 METRIC = "particle-steps/s"
 
@@ -444,7 +444,7 @@ def run_gpu(args, rank, world, local, pgroup):
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "sph_list_pass_kernel (momentum pass)", "peak_source": peak_src,
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one momentum-pass "
-                                           "launch at 1,000,000 particles (508 B per particle), scaled by N"
+                                           "launch at 1,000,000 particles (511 B per particle), scaled by N"
                          if traffic else None,
                          "bytes_per_particle": bpp,
                          "binding_resource": "FP32 issue (double-word f64 arithmetic)" if args.mode == "fast"
