@@ -11,10 +11,11 @@ Output: one JSON line (rank 0).  `value` = particle-steps/s over the timed steps
 resident in HBM (CUDA events on the library's stream, max over ranks); `e2e` = the same metric
 through the public C ABI with host buffers (pinned) copied in and out every step, pipelined
 with the asynchronous field calls so the copies overlap the neighbouring steps.  `roofline`
-describes the momentum pass (the step's dominant kernel).  Unless --no-extras, three more
+describes the momentum pass (the step's dominant kernel).  Unless --no-extras, four more
 sections on rank 0: `batched` (512 uneven 2D dam breaks in one handle vs looping the plain
-handles), `adjoint` (backward / forward cost of the differentiable 3D workload) and `dem`
-(200,000-sphere settling).
+handles), `adjoint` (backward / forward cost of the differentiable 3D workload), `dem`
+(200,000-sphere settling) and `sweep` (the lattice at 256k, 1M and 4M particles in f64 and f32,
+double-word / fast and IEEE arithmetic).
 
 `--impl reference` times the CPU path on the host cores instead: the reference has no executable
 particle path (its code generator returns text, prestige/src/codegen/simple_cpu.rs:3-22), so the
@@ -64,7 +65,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the batched, adjoint and DEM sections")
     p.add_argument("--no-autotune", action="store_true", help="keep the default block size and cell multiplier")
-    p.add_argument("--section", default="all", choices=["all", "batched", "adjoint", "dem"],
+    p.add_argument("--section", default="all", choices=["all", "batched", "adjoint", "dem", "sweep"],
                    help="run only one extra section and print its JSON (for profiling)")
     p.add_argument("--adjoint-steps", type=int, default=500)
     p.add_argument("--adjoint-every", type=int, default=50)
@@ -335,6 +336,33 @@ def bench_dem(steps=30):
             "contacts_last_step": contacts}
 
 
+def bench_sweep(steps=100, warmup=3, sizes=(262144, 1000000, 4096000)):
+    """The 3D lattice sweep over N and arithmetic: device-timed steps (CUDA events on the
+    library's stream), block 256 and cell multiplier 0.5 for every case."""
+    from prestige_gb300 import ParticleSystem, make_config, workloads
+    cases = [("f64", 1, "double-word"), ("f64", 0, "IEEE"), ("f32", 1, "fast (FMA)"), ("f32", 0, "IEEE")]
+    rows = []
+    for n in sizes:
+        for prec, mode, label in cases:
+            w = workloads.sph_lattice_3d(n=n, seed=2, precision=1 if prec == "f64" else 0, f64_mode=mode)
+            s = ParticleSystem(make_config(**w["config"]), w["n"])
+            workloads.load_into(s, w)
+            s.set_tuning(256, 0.5, mode)
+            s.step(warmup)
+            s.timing_enable(True)
+            s.step_async(steps)
+            s.sync()
+            t = s.timing_read()
+            s.timing_enable(False)
+            s.close()
+            ms = t["region_ms"] / steps
+            rows.append({"particles": w["n"], "precision": prec, "arith": label, "ms_per_step": ms,
+                         "value": w["n"] / (ms * 1e-3)})
+    return {"workload": "jittered cubic lattice, dx=0.01, jitter +-0.2dx, h=1.3dx, v ~ N(0, 0.1), "
+                        "rho = 1000(1 + U(-0.01, 0.01)), seed 2", "steps": steps, "unit": "particle-steps/s",
+            "tuning": "block 256, cell multiplier 0.5", "results": rows}
+
+
 def run_gpu(args, rank, world, local, pgroup):
     import torch
 
@@ -346,7 +374,7 @@ def run_gpu(args, rank, world, local, pgroup):
             if args.section == "adjoint":
                 res = bench_adjoint(args.adjoint_steps, args.adjoint_every, modes=args.adjoint_modes.split(","))
             else:
-                res = {"batched": bench_batched, "dem": bench_dem}[args.section]()
+                res = {"batched": bench_batched, "dem": bench_dem, "sweep": bench_sweep}[args.section]()
             print(json.dumps({"section": args.section, args.section: res}), flush=True)
         return
     w = workload(args)
@@ -463,6 +491,7 @@ def run_gpu(args, rank, world, local, pgroup):
             out["adjoint"] = bench_adjoint(args.adjoint_steps, args.adjoint_every,
                                            modes=args.adjoint_modes.split(","))
             out["dem"] = bench_dem()
+            out["sweep"] = bench_sweep()
         print(json.dumps(out), flush=True)
 
 
