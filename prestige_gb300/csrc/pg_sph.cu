@@ -78,9 +78,12 @@ __global__ void sph_gather_real(SphArgs a) {
   if (sizeof(R) == 8) ((float4*)a.s[3])[k] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
 }
 
-// Double-word copies for the f64 fast mode:
-//   s0 {x,y,z,m}.hi  s1 {x,y,z,m}.lo  s2 {vx,vy,vz,0}.hi  s3 {vx,vy,vz,0}.lo
-//   s4 {rho.hi, rho.lo, P.hi, P.lo}   s5 double {x,y,z} for the exact neighbour test near the cut-off.
+// Packs of the f64 fast (double-word) mode:
+//   s0 {x,y,z,m}.hi (the list kernel's FP32 positions)
+//   s1 DfRecord {x,y,z,m}.hi, {x,y,z,m}.lo, {vx,vy,vz,0}.hi, {vx,vy,vz,0}.lo (the pair passes)
+//   s4 {rho.hi, rho.lo, P.hi, P.lo}   s5 double {x,y,z} for the exact neighbour test near 2h.
+// Positions in s0 and s1 are shifted (see sph_gather_df).
+
 // p / rho^2 of the Tait law in double-word arithmetic on the FP32 pipe (relative error about
 // 1e-12: (rho/rho0)^gamma - 1 loses the digits its cancellation takes).
 __device__ __forceinline__ df tait_pterm_df(const SphDF& w, int gamma, df rho) {

@@ -174,15 +174,18 @@ __device__ __forceinline__ void classify(const float4& pi, const float4& pj, flo
 // Neighbour lists.  sph_list_kernel walks the candidates of every slot once per step and writes
 // the listed slots (classify: the FP32 superset, or with XD >= 0 exactly the f64 neighbours;
 // never the slot itself) in walk order (rows z, then y ascending; slots ascending along a row)
-// to nlist[k * cap ...]; nlen[k] = number of listed slots (may exceed cap).  When the list fills,
-// nresume[2k], [2k+1] = (row, slot) of the first listed candidate that did not fit, so the pair
-// passes can continue the walk from there.
+// to nlist in warp tiles (list_base: entry q of the 32 slots of a tile is one 128-byte line, so a
+// warp's reads of one entry index coalesce and its writes fill whole sectors while they are in
+// L2); nlen[k] = number of listed slots (may exceed cap).  When the list fills, nresume[2k],
+// [2k+1] = (row, slot) of the first listed candidate that did not fit, so the pair passes can
+// continue the walk from there.
 //
-// Each lane walks its own rows, kListBatch candidates at a time: loads without a clamp (the packs are padded by kPackPad records), the
-// FP32 classification folded into bit masks, the rare f64 band tests once per batch, then the
-// pushes of the batch's hits in order.  Lanes whose targets share a cell walk the same
-// candidates in step, so their loads coalesce (pruning each lane's rows to the cells its own
-// target can reach was measured: it breaks that, and the walk got slower).
+// Each lane walks its own rows, kListBatch candidates at a time: loads without a clamp (the
+// packs are padded by kPackPad records), the FP32 classification folded into bit masks, the rare
+// f64 band tests once per batch, then the pushes of the batch's hits in order.  The next row's
+// slot range is loaded while the current row is walked.  Lanes whose targets share a cell walk
+// the same candidates in step, so their loads coalesce (pruning each lane's rows to the cells
+// its own target can reach was measured: it breaks that, and the walk got slower).
 // ---------------------------------------------------------------------------------------
 constexpr int kListBatch = 8;
 
