@@ -479,11 +479,15 @@ def run_gpu(args, rank, world, local, pgroup):
                          and args.precision == "f64" else ("FP64 pipe" if args.precision == "f64" else "FP32 issue")},
             "stages_ms_per_step": {"neighbor_search": t["neighbor_ms"] / K, "sorted_gather": t["gather_ms"] / K,
                                    "neighbor_lists": list_ms, "continuity_pass": cont_ms, "momentum_pass": mom_ms},
+            "stages_note": ("overlapped: neighbor_lists = lists of the first %d slots; continuity_pass = the "
+                            "continuity pass over them beside the lists of the rest (second stream), then the "
+                            "continuity pass over the rest" % info["overlap_split"]) if info.get("overlap_split")
+            else "sequential stages",
             "gpu_launches": int(t["launches"]),
             "clocks": clk,
             "cpu_baseline": cpu,
             "info": {"n_cells": info["n_cells"], "sort_passes": info["sort_passes"], "pass_grid": info["pass_grid"],
-                     "arith": info["arith"]},
+                     "arith": info["arith"], "overlap_split": info.get("overlap_split", 0)},
             "tuning": tuning,
         }
         if not args.no_extras:

@@ -91,6 +91,8 @@ typedef struct pg_info {
   double grid_lo[3];
   double cell_size;
   int list_capacity;  /* entries per particle of the pair-pass neighbour lists */
+  long long overlap_split;  /* > 0: the continuity pass over slots [0, split) runs beside the
+                               neighbour lists of [split, n) (double-word SPH handles) */
 } pg_info;
 
 /* Fill *cfg with defaults (3D f64 SPH, gamma 7, alpha 0.1, eps 0.01, multiplier 1). */

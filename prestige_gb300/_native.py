@@ -44,7 +44,7 @@ class PgInfo(ctypes.Structure):
         ("n_cells", ctypes.c_longlong),
         ("reach", ctypes.c_int), ("pass_grid", ctypes.c_int), ("sort_passes", ctypes.c_int), ("graph", ctypes.c_int),
         ("grid_n", ctypes.c_int * 3), ("grid_lo", _d3), ("cell_size", ctypes.c_double),
-        ("list_capacity", ctypes.c_int),
+        ("list_capacity", ctypes.c_int), ("overlap_split", ctypes.c_longlong),
     ]
 
 

@@ -82,6 +82,8 @@ struct SphArgs {
   uint32_t* nlen;            // neighbours of slot k that passed the prefilter (may exceed cap)
   uint32_t* nresume;         // (row, slot) where the walk continues when nlen[k] > cap
   uint32_t cap;
+  uint32_t k_begin, k_end;   // sorted slots handled by the list and pair kernels (k_begin a multiple
+                             // of the block size; the whole system is [0, n))
   unsigned* err;             // device error word (ERR_* bits)
   int integrate;
 };
@@ -91,6 +93,7 @@ int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith);
 // block: threads per block (multiple of 32, <= kSphMaxThreads).
 int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid, int block);
 int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid, int block);
+int sph_list_regs(int arith, int dim, int stage);  // registers per thread of a list kernel (stage < 0) or pass
 int sph_list_occupancy(int arith, int dim, int stage, int block);  // stage < 0: the list kernel
 // The list kernel with an explicit FP32 prefilter-position pack a.s[pf_index] (conservative test).
 int launch_sph_list_pf(cudaStream_t st, const SphArgs& a, int pf_index, int grid, int block);

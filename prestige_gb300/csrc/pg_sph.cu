@@ -470,8 +470,12 @@ int launch_table(cudaStream_t st, const SphArgs& a, PassKernel kern, int pf, int
     set_error("block size %d must be a multiple of 32 in 32..%d", block, kSphMaxThreads);
     return PG_EINVAL;
   }
-  if (a.n == 0) return PG_OK;
-  const uint32_t ntiles = (a.n + block - 1) / block;
+  if (a.k_begin % (uint32_t)block || a.k_end > a.n || a.k_begin > a.k_end) {
+    set_error("slot range [%u, %u) does not fit block size %d and n = %u", a.k_begin, a.k_end, block, a.n);
+    return PG_EINVAL;
+  }
+  if (a.k_end == a.k_begin) return PG_OK;
+  const uint32_t ntiles = (a.k_end + block - 1) / block - a.k_begin / block;
   if (grid <= 0 || (uint32_t)grid > ntiles) grid = (int)ntiles;
   kern<<<grid, block, 0, st>>>(a, pf);
   PG_CUDA_TRY(cudaGetLastError());
@@ -540,6 +544,14 @@ int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage
   int pf = 0;
   PassKernel kern = list_kernel(arith, a.dim, stage, &pf);
   return launch_table(st, a, kern, pf, grid, block);
+}
+
+int sph_list_regs(int arith, int dim, int stage) {
+  int pf = 0;
+  PassKernel kern = list_kernel(arith, dim, stage, &pf);
+  cudaFuncAttributes attr;
+  if (!kern || cudaFuncGetAttributes(&attr, kern) != cudaSuccess) return 0;
+  return attr.numRegs;
 }
 
 int sph_list_occupancy(int arith, int dim, int stage, int block) {

@@ -54,7 +54,7 @@ struct Target {
 
 __device__ __forceinline__ Target target_of(const SphArgs& a, uint32_t k0, const SphK** Kp, int R) {
   Target T;
-  T.live = k0 < a.n;
+  T.live = k0 < a.k_end;
   T.k = T.live ? k0 : a.n - 1;
   T.id = a.sorted_id[T.k];
   const SphK& K = a.sys[sys_of_slot(a, T.id)];
@@ -216,9 +216,9 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_kernel(SphArgs a, int
   const int side = 2 * R + 1;
   const int nrows = side * (2 * RZ + 1);
   const uint32_t bs = blockDim.x;
-  const uint32_t ntiles = (a.n + bs - 1) / bs;
+  const uint32_t tile1 = (a.k_end + bs - 1) / bs;
 
-  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  for (uint32_t tile = a.k_begin / bs + blockIdx.x; tile < tile1; tile += gridDim.x) {
     const SphK* Kp;
     const Target T = target_of(a, tile * bs + tid, &Kp, R);
     const SphK& K = *Kp;
@@ -298,10 +298,10 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_pass_kernel(SphArgs a
   const int tid = threadIdx.x;
   const uint32_t cap = a.cap;
   const uint32_t bs = blockDim.x;
-  const uint32_t ntiles = (a.n + bs - 1) / bs;
-  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  const uint32_t tile1 = (a.k_end + bs - 1) / bs;
+  for (uint32_t tile = a.k_begin / bs + blockIdx.x; tile < tile1; tile += gridDim.x) {
     const uint32_t k0 = tile * bs + tid;
-    const bool live = k0 < a.n;
+    const bool live = k0 < a.k_end;
     const uint32_t k = live ? k0 : a.n - 1;
     const uint32_t id = a.sorted_id[k];
     const SphK& K = a.sys[sys_of_slot(a, id)];

@@ -51,6 +51,12 @@ struct pg_system {
   int list_grid = 0;
   int block = 128;               // threads per block of the list-based SPH kernels
   int list_cap = 128;            // neighbour-list slots per particle
+  // overlap of the continuity pass over slots [0, split) with the list kernel over [split, n) on
+  // the auxiliary stream (split 0: off); reduced persistent grids let both kernels share the SMs
+  uint32_t ov_split = 0;
+  int ov_pass_grid = 0, ov_list_grid = 0;
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ov_ev[2] = {nullptr, nullptr};
   pg::DevBuf nlist, nlen, nresume;
   pg::DevBuf posmin;             // 3 x u64, double-word mode (pos_min_kernel)
   double pos_pad = 0.0;          // 8 x the largest h of the handle's systems
