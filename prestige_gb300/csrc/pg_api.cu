@@ -438,15 +438,16 @@ int capture_graphs(pg_system* s) {
 }
 
 // Overlap of the continuity pass (FMA-bound) with the list kernel (ALU-bound) for double-word
-// SPH handles of at least 64k particles: the lists of the first 70 % of the slots are built
+// SPH handles of at least 1M particles: the lists of the first 70 % of the slots are built
 // first, then the continuity pass over them runs beside the lists of the rest.  The two
 // kernels' persistent grids are sized so that their blocks fit on an SM together (two thirds of
 // the pass's blocks, registers per block from the kernels' attributes).  Measured at 4M
 // particles: 9.27 ms per step against 9.46 without the overlap; splits of 0.35 and 0.5 and a
-// single pass block per SM were slower.
+// single pass block per SM were slower.  At 1M particles it is even (2.37 against 2.40 ms), at
+// 256k slower (0.81 against 0.75 ms), hence the threshold.
 int choose_overlap(pg_system* s, int sms) {
   s->ov_split = 0;
-  if (s->model != PG_MODEL_SPH || s->arith != ARITH_F64_DF || s->n < 65536) return PG_OK;
+  if (s->model != PG_MODEL_SPH || s->arith != ARITH_F64_DF || s->n < 1000000) return PG_OK;
   const int rp = sph_list_regs(s->arith, s->dim, SPH_CONT), rl = sph_list_regs(s->arith, s->dim, -1);
   if (rp <= 0 || rl <= 0) return PG_OK;
   const int per_block_p = ((rp + 7) / 8) * 8 * s->block, per_block_l = ((rl + 7) / 8) * 8 * s->block;

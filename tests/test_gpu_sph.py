@@ -198,10 +198,10 @@ def test_steps_bit_exact_across_cell_sizes(pg, oracle, mult):
 
 
 def test_overlapped_continuity_and_lists_match_the_oracle(pg, oracle):
-    """Above 64k particles a double-word step runs the continuity pass over the first half of the
-    slots beside the neighbour lists of the second half (two streams); the step must still
-    match the oracle, and replaying it as a CUDA graph must give the same bits."""
-    w = workloads.sph_lattice_3d(n=80000, seed=13)
+    """From 1M particles a double-word step runs the continuity pass over the first 70 % of the
+    slots beside the neighbour lists of the rest (two streams); the step must still match the
+    oracle, and replaying it as a CUDA graph must give the same bits."""
+    w = workloads.sph_lattice_3d(n=1000000, seed=13)
     s, cfg = _pair(w, 1, 1)
     assert s.info()["overlap_split"] > 0
     st = _ostate(oracle, w)
