@@ -444,10 +444,12 @@ int capture_graphs(pg_system* s) {
 // the pass's blocks, registers per block from the kernels' attributes).  Measured at 4M
 // particles: 9.27 ms per step against 9.46 without the overlap; splits of 0.35 and 0.5 and a
 // single pass block per SM were slower.  At 1M particles it is even (2.37 against 2.40 ms), at
-// 256k slower (0.81 against 0.75 ms), hence the threshold.
+// 256k slower (0.81 against 0.75 ms), hence the threshold; the 512-system batch of 2D dam
+// breaks (6.1M particles) was slower with it too (3.91 against 3.81 ms), so batched handles
+// keep the sequential schedule.
 int choose_overlap(pg_system* s, int sms) {
   s->ov_split = 0;
-  if (s->model != PG_MODEL_SPH || s->arith != ARITH_F64_DF || s->n < 1000000) return PG_OK;
+  if (s->model != PG_MODEL_SPH || s->arith != ARITH_F64_DF || s->n < 1000000 || s->nsys > 1) return PG_OK;
   const int rp = sph_list_regs(s->arith, s->dim, SPH_CONT), rl = sph_list_regs(s->arith, s->dim, -1);
   if (rp <= 0 || rl <= 0) return PG_OK;
   const int per_block_p = ((rp + 7) / 8) * 8 * s->block, per_block_l = ((rl + 7) / 8) * 8 * s->block;
