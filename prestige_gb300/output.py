@@ -1,12 +1,15 @@
-"""Particle-state output: legacy VTK polydata and CSV, written on the host.
+"""Particle-state output: legacy VTK polydata, Gmsh MSH and CSV, written on the host.
 
-The reference anticipates these formats (its .gitignore lists *.vtk and *.csv) but has no
-writer.  Both functions take named arrays in particle-id order (a ParticleSystem's `get`
+The reference anticipates these formats (its .gitignore lists *.vtk, *.msh and *.csv) but has
+no writer.  The functions take named arrays in particle-id order (a ParticleSystem's `get`
 results, or any arrays of the same shape), so no device code is involved.
 
   write_vtk(path, pos, fields)   legacy VTK 3.0, binary (big-endian float64), POLYDATA with one
                                  vertex per particle; scalars as SCALARS, n x dim arrays as
                                  VECTORS (2D vectors padded with z = 0)
+  write_msh(path, pos, fields)   Gmsh MSH 2.2 (ASCII): one node and one point element (type 15)
+                                 per particle, each field as a $NodeData block (1 or 3
+                                 components, 2D vectors padded with z = 0), values in %.17g
   write_csv(path, pos, fields)   header x,y[,z],<field>[_x,_y,_z]...; one row per particle
   snapshot(system, names)        positions and the named slices of a ParticleSystem
 """
@@ -60,6 +63,32 @@ def write_vtk(path, pos, fields=None, title="prestige particles"):
             else:
                 raise ValueError("field %r must be n or n x 2/3" % name)
             f.write(b"\n")
+
+
+def write_msh(path, pos, fields=None, time=0.0, step=0):
+    pts = _points3(pos)
+    n = pts.shape[0]
+    cols = _columns(n, fields or {})
+    ids = np.arange(1, n + 1)
+    with open(path, "w") as f:
+        f.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n")
+        f.write("$Nodes\n%d\n" % n)
+        np.savetxt(f, np.column_stack([ids, pts]), fmt=["%d", "%.17g", "%.17g", "%.17g"])
+        f.write("$EndNodes\n$Elements\n%d\n" % n)
+        np.savetxt(f, np.column_stack([ids, np.full(n, 15), np.full(n, 2), np.zeros(n, int), np.ones(n, int), ids]),
+                   fmt="%d")
+        f.write("$EndElements\n")
+        for name, a in cols:
+            if a.ndim == 1:
+                vals = a[:, None]
+            elif a.ndim == 2 and a.shape[1] in (2, 3):
+                vals = _points3(a)
+            else:
+                raise ValueError("field %r must be n or n x 2/3" % name)
+            f.write('$NodeData\n1\n"%s"\n1\n%.17g\n3\n%d\n%d\n%d\n' % (name.replace('"', "'"), time, step,
+                                                                        vals.shape[1], n))
+            np.savetxt(f, np.column_stack([ids, vals]), fmt=["%d"] + ["%.17g"] * vals.shape[1])
+            f.write("$EndNodeData\n")
 
 
 def write_csv(path, pos, fields=None):

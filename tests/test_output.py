@@ -1,4 +1,4 @@
-"""Host-side VTK and CSV writers of particle state (prestige_gb300.output); no GPU."""
+"""Host-side VTK, Gmsh MSH and CSV writers of particle state (prestige_gb300.output); no GPU."""
 import numpy as np
 
 from prestige_gb300 import output
@@ -71,3 +71,54 @@ def test_rejects_mismatched_rows(tmp_path):
     import pytest
     with pytest.raises(ValueError):
         output.write_vtk(str(tmp_path / "d.vtk"), np.zeros((4, 3)), {"rho": np.zeros(5)})
+
+
+def _read_msh(path):
+    lines = open(path).read().split("\n")
+    assert lines[0] == "$MeshFormat" and lines[1] == "2.2 0 8"
+    i = lines.index("$Nodes")
+    n = int(lines[i + 1])
+    nodes = np.array([[float(v) for v in l.split()] for l in lines[i + 2:i + 2 + n]])
+    assert lines[i + 2 + n] == "$EndNodes"
+    j = lines.index("$Elements")
+    assert int(lines[j + 1]) == n
+    el = np.array([[int(v) for v in l.split()] for l in lines[j + 2:j + 2 + n]])
+    assert (el[:, 1] == 15).all() and (el[:, 5] == np.arange(1, n + 1)).all()
+    out = {"ids": nodes[:, 0], "points": nodes[:, 1:]}
+    k = j + 2 + n
+    while True:
+        try:
+            k = lines.index("$NodeData", k)
+        except ValueError:
+            break
+        name = lines[k + 2].strip('"')
+        comps, count = int(lines[k + 7]), int(lines[k + 8])
+        out[name] = np.array([[float(v) for v in l.split()[1:]] for l in lines[k + 9:k + 9 + count]])
+        if comps == 1:
+            out[name] = out[name][:, 0]
+        assert lines[k + 9 + count] == "$EndNodeData"
+        k += 9 + count
+    return out
+
+
+def test_msh_round_trip(tmp_path):
+    rng = np.random.default_rng(3)
+    pos = rng.normal(size=(23, 3))
+    vel = rng.normal(size=(23, 3))
+    rho = rng.uniform(990, 1010, size=23)
+    p = str(tmp_path / "c.msh")
+    output.write_msh(p, pos, {"vel": vel, "rho": rho}, time=0.5, step=7)
+    back = _read_msh(p)
+    assert np.array_equal(back["ids"], np.arange(1, 24))
+    assert np.array_equal(back["points"], pos)
+    assert np.array_equal(back["vel"], vel)
+    assert np.array_equal(back["rho"], rho)
+
+
+def test_msh_2d_pads_z(tmp_path):
+    pos = np.arange(12.0).reshape(6, 2)
+    p = str(tmp_path / "d.msh")
+    output.write_msh(p, pos, {"v": pos})
+    back = _read_msh(p)
+    assert np.array_equal(back["points"][:, :2], pos) and np.all(back["points"][:, 2] == 0)
+    assert np.array_equal(back["v"][:, :2], pos) and np.all(back["v"][:, 2] == 0)
