@@ -223,13 +223,12 @@ struct RealPairs {
     const R4 Bj = p.b;
     const R r = Ops::sqrt(r2);
     const R q = Ops::mul(r, c.inv_h);
-    R F;
-    if (q < R(1)) {
-      F = Ops::mul(c.fa, Ops::sub(Ops::mul(R(2.25), q), R(3)));
-    } else {
-      const R tq = Ops::sub(R(2), q);
-      F = Ops::div(Ops::mul(c.fb, Ops::mul(tq, tq)), r);
-    }
+    // both pieces of the spline in the oracle's operation order, then a select (no divergence;
+    // the selected value is bit for bit the oracle's)
+    const R tq = Ops::sub(R(2), q);
+    const R Fnear = Ops::mul(c.fa, Ops::sub(Ops::mul(R(2.25), q), R(3)));
+    const R Ffar = Ops::div(Ops::mul(c.fb, Ops::mul(tq, tq)), r);
+    const R F = q < R(1) ? Fnear : Ffar;
     const R dv0 = Ops::sub(vi[0], Bj.x), dv1 = Ops::sub(vi[1], Bj.y);
     const R dv2 = DIM == 3 ? Ops::sub(vi[2], Bj.z) : R(0);
     R w = Ops::add(Ops::mul(dv0, d0), Ops::mul(dv1, d1));
@@ -238,8 +237,8 @@ struct RealPairs {
     if (kCont) dr = Ops::add(dr, Ops::mul(mj, Ops::mul(w, F)));
     if (kMom) {
       const R2 qj = p.q;
-      R pij = R(0);
-      if (w < R(0)) pij = Ops::div(Ops::mul(c.avk, w), Ops::mul(Ops::add(r2, c.eps_h2), Ops::add(rhoi, qj.x)));
+      const R av = Ops::div(Ops::mul(c.avk, w), Ops::mul(Ops::add(r2, c.eps_h2), Ops::add(rhoi, qj.x)));
+      const R pij = w < R(0) ? av : R(0);
       const R coef = Ops::mul(mj, Ops::mul(Ops::add(Ops::add(Pi, qj.y), pij), F));
       acc[0] = Ops::sub(acc[0], Ops::mul(coef, d0));
       acc[1] = Ops::sub(acc[1], Ops::mul(coef, d1));
