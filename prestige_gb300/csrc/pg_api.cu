@@ -1241,8 +1241,23 @@ int pg_dem_set_history(pg_system* s, const uint32_t* partner, const double* xi, 
   const size_t C = capacity;
   PG_CUDA_TRY(cudaStreamSynchronize(s->stream));
   if (s->n) {
-    PG_CUDA_TRY(cudaMemcpy(s->hpid[s->hcur].p, partner, 4 * s->n * C, cudaMemcpyHostToDevice));
-    PG_CUDA_TRY(cudaMemcpy(s->hxi[s->hcur].p, xi, 8 * s->n * C * 3, cudaMemcpyHostToDevice));
+    // a particle's history ends at its first empty slot; every slot after it is stored empty
+    // (no partner, zero spring), the form the contact pass keeps and the oracle produces
+    std::vector<uint32_t> p(partner, partner + s->n * C);
+    std::vector<double> x(xi, xi + s->n * C * 3);
+    for (size_t i = 0; i < s->n; ++i) {
+      bool ended = false;
+      for (size_t k = 0; k < C; ++k) {
+        const size_t o = i * C + k;
+        ended = ended || p[o] == 0xFFFFFFFFu;
+        if (ended) {
+          p[o] = 0xFFFFFFFFu;
+          x[3 * o] = x[3 * o + 1] = x[3 * o + 2] = 0.0;
+        }
+      }
+    }
+    PG_CUDA_TRY(cudaMemcpy(s->hpid[s->hcur].p, p.data(), 4 * s->n * C, cudaMemcpyHostToDevice));
+    PG_CUDA_TRY(cudaMemcpy(s->hxi[s->hcur].p, x.data(), 8 * s->n * C * 3, cudaMemcpyHostToDevice));
   }
   return PG_OK;
 }

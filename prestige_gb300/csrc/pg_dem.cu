@@ -147,14 +147,24 @@ __global__ void __launch_bounds__(128) dem_pass_kernel(DemArgs a) {
     const int cz = (int)(c / ((uint32_t)g.nx * (uint32_t)g.ny));
     const int R = a.reach;
     const int x0 = max(cx - R, 0), x1 = min(cx + R, g.nx - 1);
-    for (int dz = -R; dz <= R; ++dz) {
-      const int z = cz + dz;
-      if (z < 0 || z >= g.nz) continue;
-      for (int dy = -R; dy <= R; ++dy) {
-        const int y = cy + dy;
-        if (y < 0 || y >= g.ny) continue;
+    const int side = 2 * R + 1, nrows = side * side;
+    // slot range of a row of cells (empty outside the grid); the next row's range is loaded
+    // while the current row is walked
+    auto row_range = [&](int r, uint32_t& b, uint32_t& e) {
+      const int z = cz + r / side - R, y = cy + r % side - R;
+      b = e = 0;
+      if (z >= 0 && z < g.nz && y >= 0 && y < g.ny) {
         const uint32_t rb = g.cell_base + ((uint32_t)z * g.ny + (uint32_t)y) * g.nx;
-        const uint32_t s0 = a.cell_start[rb + x0], e0 = a.cell_start[rb + x1 + 1];
+        b = a.cell_start[rb + x0];
+        e = a.cell_start[rb + x1 + 1];
+      }
+    };
+    uint32_t nb, ne;
+    row_range(0, nb, ne);
+    for (int row = 0; row < nrows; ++row) {
+      const uint32_t s0 = nb, e0 = ne;
+      if (row + 1 < nrows) row_range(row + 1, nb, ne);
+      {
         for (uint32_t t = s0; t < e0; ++t) {
           {
             const float4 fj = a.sF[t];
@@ -216,7 +226,12 @@ __global__ void __launch_bounds__(128) dem_pass_kernel(DemArgs a) {
       contact_law(K, ct, xo, F, T, xn);
       store(kWallId + (uint32_t)face, xn);
     }
+    // Slots after the last contact must read as empty.  The buffer being written held this
+    // particle's history of two steps ago, and every history buffer is empty after its first
+    // empty slot (initial state, pg_dem_set_history and this loop keep that), so only the
+    // slots up to the old history's end need clearing: usually a single load.
     for (int s = slot; s < C; ++s) {
+      if (hp_new[s] == kNoPartner) break;
       hp_new[s] = kNoPartner;
       hx_new[s * 3] = 0.0;
       hx_new[s * 3 + 1] = 0.0;
@@ -224,15 +239,21 @@ __global__ void __launch_bounds__(128) dem_pass_kernel(DemArgs a) {
     }
     if (overflow) atomicOr(a.err, ERR_CONTACT_OVERFLOW);
 
-    // symplectic Euler: v' = v + dt (F/m + g); x' = x + dt v'; w' = w + dt T / (0.4 m r^2)
-    const double I = dmul(dmul(dmul(0.4, mi), ri), ri);
+    // symplectic Euler: v' = v + dt (F/m + g); x' = x + dt v'; w' = w + dt T / (0.4 m r^2).
+    // A particle without contacts has F = T = 0, and 0 / d is that zero (sign kept) for a
+    // positive finite d, so those quotients skip the f64 division (1/64-rate pipe on GB300)
+    // without changing a bit.
     const size_t o = (size_t)id * 3;
+    const double I = dmul(dmul(dmul(0.4, mi), ri), ri);
+    const bool m_ok = mi > 0.0 && mi < INFINITY, i_ok = I > 0.0 && I < INFINITY;
 #pragma unroll
     for (int cc = 0; cc < 3; ++cc) {
-      const double v = dadd(vi[cc], dmul(K.dt, dadd(ddiv(F[cc], mi), K.grav[cc])));
+      const double fm = (F[cc] == 0.0 && m_ok) ? F[cc] : ddiv(F[cc], mi);
+      const double v = dadd(vi[cc], dmul(K.dt, dadd(fm, K.grav[cc])));
       a.vel[o + cc] = v;
       a.pos[o + cc] = dadd(xi[cc], dmul(K.dt, v));
-      a.omega[o + cc] = dadd(wi[cc], dmul(K.dt, ddiv(T[cc], I)));
+      const double ti = (T[cc] == 0.0 && i_ok) ? T[cc] : ddiv(T[cc], I);
+      a.omega[o + cc] = dadd(wi[cc], dmul(K.dt, ti));
     }
   }
   // contact count: warp sum, one atomic per warp
