@@ -568,8 +568,11 @@ int setup_system(pg_system* s) {
       k.grav[d] = c.gravity[d];
       k.wall_lo[d] = c.wall_lo[d];
       k.wall_hi[d] = c.wall_hi[d];
+      k.wall_lo_f[d] = (float)c.wall_lo[d];
+      k.wall_hi_f[d] = (float)c.wall_hi[d];
     }
     k.capacity = c.contact_capacity;
+    k.dt_finite = std::isfinite(c.dt) ? 1 : 0;
     PG_TRY(s->demk.ensure(sizeof(DemK)));
     PG_CUDA_TRY(cudaMemcpy(s->demk.p, &k, sizeof(DemK), cudaMemcpyHostToDevice));
     PG_TRY(s->pos.ensure(8 * n * 3));

@@ -33,6 +33,13 @@ __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a,
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
 
+// +-0 and 0 < x < inf, tested on the bit pattern.
+__device__ __forceinline__ bool is_zero(double x) { return ((unsigned long long)__double_as_longlong(x) << 1) == 0; }
+__device__ __forceinline__ bool positive_finite(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return b != 0 && (b >> 52) < 0x7ffull;  // sign clear, not zero, exponent below inf/NaN
+}
+
 __device__ __forceinline__ void cross3(const double* a, const double* b, double* c) {
   c[0] = dsub(dmul(a[1], b[2]), dmul(a[2], b[1]));
   c[1] = dsub(dmul(a[2], b[0]), dmul(a[0], b[2]));
@@ -207,6 +214,15 @@ __global__ void __launch_bounds__(128) dem_pass_kernel(DemArgs a) {
     for (int face = 0; face < 6; ++face) {
       const int ax = face / 2;
       const bool hi_face = face & 1;
+      // FP32 screen: with every rounding of the FP32 copies bounded (slack), a particle that
+      // fails it has dist >= r in f64 as well, so the f64 test is needed only near a wall
+      {
+        const float xf = ax == 0 ? fi.x : ax == 1 ? fi.y : fi.z;
+        const float wf = hi_face ? K.wall_hi_f[ax] : K.wall_lo_f[ax];
+        const float df = hi_face ? wf - xf : xf - wf;
+        const float wslack = 2.384185791015625e-07f * (2.f * (fabsf(xf) + fabsf(wf)) + fi.w) + 1.0e-6f * fi.w;
+        if (df >= fi.w + wslack) continue;
+      }
       const double dist = hi_face ? dsub(K.wall_hi[ax], xi[ax]) : dsub(xi[ax], K.wall_lo[ax]);
       if (!(dist < ri)) continue;
       Contact ct;
@@ -243,17 +259,26 @@ __global__ void __launch_bounds__(128) dem_pass_kernel(DemArgs a) {
     // A particle without contacts has F = T = 0, and 0 / d is that zero (sign kept) for a
     // positive finite d, so those quotients skip the f64 division (1/64-rate pipe on GB300)
     // without changing a bit.
+    // The zero and range checks work on the bit patterns (integer pipe).  Without torque and
+    // with a finite dt, w' = w + dt * (+-0) is w itself unless w is +-0 (then it is computed).
     const size_t o = (size_t)id * 3;
-    const double I = dmul(dmul(dmul(0.4, mi), ri), ri);
-    const bool m_ok = mi > 0.0 && mi < INFINITY, i_ok = I > 0.0 && I < INFINITY;
+    const bool free_t = is_zero(T[0]) && is_zero(T[1]) && is_zero(T[2]);
+    const double I = free_t ? 0.0 : dmul(dmul(dmul(0.4, mi), ri), ri);
+    const bool m_ok = positive_finite(mi);
 #pragma unroll
     for (int cc = 0; cc < 3; ++cc) {
-      const double fm = (F[cc] == 0.0 && m_ok) ? F[cc] : ddiv(F[cc], mi);
+      const double fm = (is_zero(F[cc]) && m_ok) ? F[cc] : ddiv(F[cc], mi);
       const double v = dadd(vi[cc], dmul(K.dt, dadd(fm, K.grav[cc])));
       a.vel[o + cc] = v;
       a.pos[o + cc] = dadd(xi[cc], dmul(K.dt, v));
-      const double ti = (T[cc] == 0.0 && i_ok) ? T[cc] : ddiv(T[cc], I);
-      a.omega[o + cc] = dadd(wi[cc], dmul(K.dt, ti));
+    }
+    if (free_t && K.dt_finite && positive_finite(dmul(dmul(dmul(0.4, mi), ri), ri))) {
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc)
+        a.omega[o + cc] = is_zero(wi[cc]) ? dadd(wi[cc], dmul(K.dt, T[cc])) : wi[cc];
+    } else {
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc) a.omega[o + cc] = dadd(wi[cc], dmul(K.dt, ddiv(T[cc], I)));
     }
   }
   // contact count: warp sum, one atomic per warp

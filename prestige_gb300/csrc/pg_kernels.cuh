@@ -135,7 +135,9 @@ struct DemK {
   GridK g;
   double kn, kt, mu, dt, gcoef;
   double grav[3], wall_lo[3], wall_hi[3];
+  float wall_lo_f[3], wall_hi_f[3];  // FP32 copies for the wall screen
   int capacity;
+  int dt_finite;
 };
 
 struct DemArgs {

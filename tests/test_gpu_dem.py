@@ -51,13 +51,30 @@ def test_dem_compressed_lattice_bit_exact(pg, oracle, graph):
 
 
 def test_dem_rsa_settling_small(pg, oracle):
+    """Free spheres (the contact-free shortcuts of the integrator), some spinning, some with a
+    signed-zero spin component, a few touching the floor."""
     w = workloads.dem_settling(n=3000, box=(0.02, 0.02, 0.06), seed=1)
+    rng = np.random.default_rng(4)
+    om = rng.normal(0.0, 20.0, size=(w["n"], 3))
+    om[::7] = 0.0
+    om[1::7, 0] = -0.0
+    w["fields"]["omega"] = om
+    pos = np.array(w["fields"]["pos"], copy=True)
+    low = np.argsort(pos[:, 2])[:20]
+    pos[low, 2] = w["fields"]["radius"][low] * (1.0 - 1e-3)  # slightly into the floor
+    w["fields"]["pos"] = pos
     s = _run_pair(w, 0, 0)
     st = _ostate(oracle, w)
     s.step(10)
     oracle.dem_run(w["config"], st, 10)
     assert np.array_equal(s.get("pos"), st.pos)
     assert np.array_equal(s.get("vel"), st.vel)
+    got = np.ascontiguousarray(s.get("omega"), np.float64).reshape(-1).view(np.uint64)
+    ref = np.ascontiguousarray(st.omega, np.float64).reshape(-1).view(np.uint64)
+    assert np.array_equal(got, ref)  # signs of zeros too
+    pid, xi = s.dem_history()
+    assert np.array_equal(pid.reshape(-1), st.hpid)
+    assert np.array_equal(xi.reshape(-1), st.hxi)
 
 
 def test_dem_contact_overflow_reported(pg, oracle):
