@@ -11,6 +11,7 @@
 
 #include <cmath>
 
+#include "pg_arith.cuh"
 #include "pg_internal.cuh"
 #include "pg_kernels.cuh"
 
@@ -123,6 +124,26 @@ __device__ __forceinline__ int cell_coord_d(double x, double lo, double inv, int
   return (int)t;
 }
 
+// cell_coord_d's result without FP64 work in nearly every case (GB300 runs FP64 at 1/64 of the
+// FP32 rate): t = (x - lo) * inv in FP32 from the FP32 copies, with a bound E on its distance
+// from the f64 t (8u (|x| + |lo|) inv + 8u |t|, twice the first-order error of the FP32 copies
+// and operations).  When [t - E, t + E] lies inside one cell, or entirely below 0 or above n,
+// that decides the clamped floor; otherwise (near a cell boundary, NaN) the f64 formula runs.
+__device__ __forceinline__ int cell_coord_fast(double x, double lo, float lof, double inv, float invf, int n) {
+  float xf, xl;
+  df_split_fast(x, &xf, &xl);
+  const float t = (xf - lof) * invf;
+  const float E = 4.76837158203125e-07f * ((fabsf(xf) + fabsf(lof)) * invf + fabsf(t));
+  const float a = t - E, b = t + E;
+  if (b < 0.f) return 0;
+  if (a >= (float)n) return n - 1;
+  if (a >= 0.f && b < (float)n) {
+    const int ia = (int)a;
+    if (ia == (int)b) return ia;
+  }
+  return cell_coord_d(x, lo, inv, n);
+}
+
 __device__ __forceinline__ int cell_coord_f(float x, float lo, float inv, int n) {
   const float t = __fmul_rn(__fsub_rn(x, lo), inv);
   if (!(t >= 0.f)) return 0;
@@ -145,7 +166,7 @@ __global__ void hash_kernel(const GridK* __restrict__ grid, const uint32_t* __re
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       const R x = pos[(size_t)i * DIM + d];
-      if (sizeof(R) == 8) c[d] = cell_coord_d((double)x, g.lo[d], g.inv, nn[d]);
+      if (sizeof(R) == 8) c[d] = cell_coord_fast((double)x, g.lo[d], g.lof[d], g.inv, g.invf, nn[d]);
       else c[d] = cell_coord_f((float)x, g.lof[d], g.invf, nn[d]);
       if (MIN) m[d] = ordered_code((double)x);
     }

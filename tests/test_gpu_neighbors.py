@@ -122,3 +122,24 @@ def test_eq1_gather_sum(pg, oracle, name, make):
                             cfg["cell_multiplier"], True)
     assert np.array_equal(s.get("fr"), ref)
     assert counts.min() >= 1
+
+
+def test_cells_at_cell_boundaries(pg, oracle):
+    """Coordinates on and within a few ulps of cell boundaries, where the hash's FP32 shortcut
+    cannot decide the cell and the f64 formula runs: cells and order stay the oracle's."""
+    rng = np.random.default_rng(12)
+    lo, hi, h = [-0.3, 0.1, 0.0], [1.7, 2.1, 2.0], 0.05
+    cell = 2 * h
+    n = 4000
+    k = rng.integers(0, 20, size=(n, 3)).astype(np.float64)
+    pos = np.array(lo) + k * cell
+    ulps = rng.integers(-4, 5, size=(n, 3))
+    pos = pos + ulps * np.spacing(np.abs(pos) + 1e-300)
+    pos[: n // 4] += rng.uniform(0.0, cell, size=(n // 4, 3))  # a quarter away from boundaries
+    cfg = dict(model=0, dim=3, precision=1, h=h, domain_lo=lo, domain_hi=hi, tait_B=1e4)
+    s = ParticleSystem(make_config(**cfg), n)
+    s.set("pos", pos)
+    cells, ids, start = s.neighbors()
+    ocell, oid, ostart = oracle.cell_list(pos, lo, hi, 2 * h, 1.0, True)
+    assert np.array_equal(ids, oid) and np.array_equal(start, ostart)
+    assert np.array_equal(cells, ocell[oid])
