@@ -136,3 +136,24 @@ def test_pair_lists_errors(pg):
     s, _ = _system(w, 1)
     with pytest.raises(nat.PgError):
         s.pair_lists()  # nothing built yet
+
+
+def test_overflowed_lists_report_full_lengths(pg, oracle):
+    """With a list capacity below the neighbour count the lengths still count every neighbour
+    and the stored entries are the first `capacity` of the exact list."""
+    w = workloads.sph_lattice_3d(n=4096, seed=2)
+    cfg = dict(w["config"])
+    cfg.update(precision=1, f64_mode=1, list_capacity=20)
+    s = ParticleSystem(make_config(**cfg), w["n"])
+    for k in ("pos", "vel", "rho", "mass"):
+        s.set(k, np.asarray(w["fields"][k], np.float64))
+    s.compute_rates()
+    lengths, entries = s.pair_lists()
+    _, ids, _ = s.neighbors()
+    ref = _oracle_lists(oracle, w, cfg)
+    assert lengths.max() > 20
+    for k in range(w["n"]):
+        r = ref[ids[k]]
+        assert lengths[k] == len(r)
+        m = min(len(r), 20)
+        assert np.array_equal(ids[entries[k, :m]], r[:m])

@@ -214,3 +214,20 @@ def test_overlapped_continuity_and_lists_match_the_oracle(pg, oracle):
     g.enable_graph(True)
     g.step(2)
     assert np.array_equal(g.get("pos"), s.get("pos")) and np.array_equal(g.get("rho"), s.get("rho"))
+
+
+def test_overlapped_schedule_with_list_overflow(pg, oracle):
+    """The overlapped schedule (1M particles) with lists too short for the neighbourhoods: the
+    passes finish every overflowed list by walking on, in both slot ranges."""
+    w = workloads.sph_lattice_3d(n=1000000, seed=17)
+    cfg = dict(w["config"])
+    cfg.update(precision=1, f64_mode=1, list_capacity=24)
+    s = ParticleSystem(make_config(**cfg), w["n"])
+    for k in ("pos", "vel", "rho", "mass"):
+        s.set(k, np.asarray(w["fields"][k], np.float64))
+    assert s.info()["overlap_split"] > 0
+    st = _ostate(oracle, w)
+    s.step(1)
+    oracle.sph_run(cfg, st, 1)
+    assert _rel(s.get("pos"), st.pos) <= F64_TOL
+    assert _rel(s.get("rho"), st.rho) <= F64_TOL
