@@ -43,9 +43,12 @@ sys.path.insert(0, ROOT)
 # pos, vel, rho', m once and writes pos, vel once.  3D f64: 64 + 48 = 112 B; f32: 56 B.
 MOM_BYTES = {"f64": 112, "f32": 56}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per particle of one momentum-pass
-# launch, from the ncu capture summarised in profiles/sph_mom_pass_lattice3d.md (1,000,000
+# launch, from the ncu capture summarised in profiles/sph_step_df_lattice3d.md (1,000,000
 # particles, f64 double-word mode), scaled by the particle count.
 MOM_TRAFFIC_PER_PARTICLE = {"f64-fast": 511.0}
+# The resource that binds the momentum pass in that capture: FMA-pipe cycles active (% of peak,
+# sm__pipe_fma_cycles_active) and issue slots active (smsp__issue_active).
+MOM_PIPES = {"f64-fast": {"fma_pipe_active_pct": 69.9, "issue_active_pct": 78.0}}
 
 METRIC = "particle-steps/s"
 
@@ -475,6 +478,7 @@ def run_gpu(args, rank, world, local, pgroup):
                                            "launch at 1,000,000 particles (511 B per particle), scaled by N"
                          if traffic else None,
                          "bytes_per_particle": bpp,
+                         "pipes_ncu": MOM_PIPES.get("%s-%s" % (args.precision, args.mode)),
                          "binding_resource": "FP32 issue (double-word f64 arithmetic)" if args.mode == "fast"
                          and args.precision == "f64" else ("FP64 pipe" if args.precision == "f64" else "FP32 issue")},
             "stages_ms_per_step": {"neighbor_search": t["neighbor_ms"] / K, "sorted_gather": t["gather_ms"] / K,
