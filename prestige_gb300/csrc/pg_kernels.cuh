@@ -18,8 +18,9 @@ enum Arith {
 constexpr int kSphThreads = 128;     // default block size of the SPH kernels
 constexpr int kSphMaxThreads = 256;  // largest block size of the list-based kernels
 constexpr uint32_t kListTile = 32;  // slots per tile of the neighbour-list array
-constexpr size_t kPackPad = 8;       // records allocated past the end of every sorted pack: the
-                                     // list kernel's batched loads may run up to 3 past a row
+constexpr size_t kPackPad = 16;      // records allocated past the end of every sorted pack: the
+                                     // list kernel's batched loads run up to kListBatch - 1 past
+                                     // the last slot
 
 // Stages of the SPH pair pass.
 enum SphStage {

@@ -187,7 +187,8 @@ __device__ __forceinline__ void classify(const float4& pi, const float4& pj, flo
 // the same candidates in step, so their loads coalesce (pruning each lane's rows to the cells
 // its own target can reach was measured: it breaks that, and the walk got slower).
 // ---------------------------------------------------------------------------------------
-constexpr int kListBatch = 8;
+constexpr int kListBatch = 16;
+static_assert(kPackPad >= (size_t)kListBatch - 1, "sorted packs must be padded for a whole batch past the end");
 
 // Offset of slot k's entry 0 in the tiled list array (entry q at + q * kListTile).
 __device__ __forceinline__ size_t list_base(uint32_t k, uint32_t cap) {
