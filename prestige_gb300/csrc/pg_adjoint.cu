@@ -370,7 +370,7 @@ struct AdjPairsF {
   };
   static constexpr bool kPrefetch = true;
 
-  __device__ __forceinline__ Pre fetch(uint32_t t) const {
+  __device__ __forceinline__ Pre fetch(uint32_t t, uint32_t) const {
     Pre p;
     p.xh = XH[t];
     p.xl = XL[t];
@@ -386,9 +386,9 @@ struct AdjPairsF {
     return p;
   }
 
-  __device__ __forceinline__ void pair(uint32_t t) { pair_with(t, fetch(t)); }
+  __device__ __forceinline__ void pair(uint32_t t) { pair_with(t, 0, fetch(t, 0)); }
 
-  __device__ __forceinline__ void pair_with(uint32_t t, const Pre& p) {
+  __device__ __forceinline__ void pair_with(uint32_t t, uint32_t, const Pre& p) {
     const float4 xj = p.xh, xj2 = p.xl;
     float d[3];
     d[0] = (xh[0] - xj.x) + (xl[0] - xj2.x);

@@ -144,6 +144,8 @@ int ensure_sorted_buffers(pg_system* s) {
   for (int i = 0; i < 6; ++i)
     if (sz[i]) PG_TRY(s->sorted[i].ensure(sz[i] * (n + kPackPad)));
   PG_TRY(s->nlist.ensure(4 * ((n + kListTile - 1) / kListTile) * kListTile * (size_t)s->list_cap));
+  if (s->arith == ARITH_F64_DF)
+    PG_TRY(s->fcache.ensure(16 * ((n + kListTile - 1) / kListTile) * kListTile * (size_t)s->list_cap));
   PG_TRY(s->nlen.ensure(4 * n));
   PG_TRY(s->nresume.ensure(8 * n));
   PG_TRY(s->posmin.ensure(3 * sizeof(unsigned long long)));
@@ -176,6 +178,7 @@ SphArgs sph_args(pg_system* s, int integrate, bool rates) {
   a.nlist = s->nlist.as<uint32_t>();
   a.nlen = s->nlen.as<uint32_t>();
   a.nresume = s->nresume.as<uint32_t>();
+  a.fcache = s->arith == ARITH_F64_DF ? s->fcache.p : nullptr;
   a.cap = (uint32_t)s->list_cap;
   a.err = s->err.as<unsigned>();
   a.posmin = s->posmin.as<unsigned long long>();
@@ -1302,7 +1305,7 @@ int pg_memory_bytes(pg_system* s, size_t* bytes) {
                               &s->contacts, &s->err};
   for (const pg::DevBuf* d : bufs) b += d->bytes;
   for (int i = 0; i < 6; ++i) b += s->sorted[i].bytes;
-  b += s->nlist.bytes + s->nlen.bytes + s->nresume.bytes;
+  b += s->nlist.bytes + s->nlen.bytes + s->nresume.bytes + s->fcache.bytes;
   for (auto& kv : s->user) b += kv.second->bytes;
   b += s->adjoint_bytes();
   *bytes = b;

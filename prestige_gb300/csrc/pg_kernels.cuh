@@ -82,6 +82,7 @@ struct SphArgs {
                              // nlist[(k / 32) * cap * 32 + q * 32 + k % 32] (q < min(nlen[k], cap))
   uint32_t* nlen;            // neighbours of slot k that passed the prefilter (may exceed cap)
   uint32_t* nresume;         // (row, slot) where the walk continues when nlen[k] > cap
+  void* fcache;              // double-word mode: F (hi, lo) per list entry, same tiling as nlist
   uint32_t cap;
   uint32_t k_begin, k_end;   // sorted slots handled by the list and pair kernels (k_begin a multiple
                              // of the block size; the whole system is [0, n))

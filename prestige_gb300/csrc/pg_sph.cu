@@ -200,7 +200,7 @@ struct RealPairs {
   };
   static constexpr bool kPrefetch = true;
 
-  __device__ __forceinline__ Pre fetch(uint32_t t) const {
+  __device__ __forceinline__ Pre fetch(uint32_t t, uint32_t) const {
     Pre p;
     p.a = A[t];
     p.b = B[t];
@@ -208,9 +208,9 @@ struct RealPairs {
     return p;
   }
 
-  __device__ __forceinline__ void pair(uint32_t t) { pair_with(t, fetch(t)); }
+  __device__ __forceinline__ void pair(uint32_t t) { pair_with(t, 0, fetch(t, 0)); }
 
-  __device__ __forceinline__ void pair_with(uint32_t t, const Pre& p) {
+  __device__ __forceinline__ void pair_with(uint32_t t, uint32_t, const Pre& p) {
     const R4 Aj = p.a;
     const R d0 = Ops::sub(xi[0], Aj.x), d1 = Ops::sub(xi[1], Aj.y);
     const R d2 = DIM == 3 ? Ops::sub(xi[2], Aj.z) : R(0);
@@ -280,8 +280,11 @@ struct DfPairs {
   SphDF w;
   double four_h2;
   uint32_t kself;
+  float4* fc;  // per list entry {F.hi, F.lo, w.hi, w.lo}: written by the continuity pass, read by
+               // the momentum pass
   df xi[3], vi[3], rhoi, Pi;
   dfacc acc[3], dr;
+  static constexpr bool kCacheF = STAGE == SPH_CONT || STAGE == SPH_MOM;
 
   __device__ __forceinline__ void begin(const SphArgs& a, const SphK& K, uint32_t k) {
     Rec = (const DfRecord*)a.s[1];
@@ -299,6 +302,7 @@ struct DfPairs {
       Pi = df_make(rp.z, rp.w);
     }
     kself = k;
+    fc = kCacheF && a.fcache ? (float4*)a.fcache + list_base(k, a.cap) : nullptr;
     acc[0] = acc[1] = acc[2] = dfacc_zero();
     dr = dfacc_zero();
   }
@@ -309,21 +313,27 @@ struct DfPairs {
   // exact neighbour list (sph_list_kernel with f64 classification).
   // The sorted-pack records of one neighbour, loaded ahead of its pair terms.
   struct Pre {
-    float4 ah, al, bh, bl, rp;
+    float4 ah, al, bh, bl, rp, fw;
   };
   static constexpr bool kPrefetch = true;
 
-  __device__ __forceinline__ Pre fetch(uint32_t t) const {
+  __device__ __forceinline__ Pre fetch(uint32_t t, uint32_t q) const { return fetch_entry(t, q, STAGE == SPH_MOM && fc); }
+
+  // cached: list entry q of a momentum pass that reads F and w from the continuity pass
+  __device__ __forceinline__ Pre fetch_entry(uint32_t t, uint32_t q, bool cached) const {
     Pre p;
     p.ah = Rec[t].ah;
     p.al = Rec[t].al;
-    p.bh = Rec[t].bh;
-    p.bl = Rec[t].bl;
+    // the momentum pass takes w from the cache and needs no velocities of the neighbour
+    p.bh = cached ? make_float4(0.f, 0.f, 0.f, 0.f) : Rec[t].bh;
+    p.bl = cached ? make_float4(0.f, 0.f, 0.f, 0.f) : Rec[t].bl;
     p.rp = kMom ? RP[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+    p.fw = cached ? fc[q * kListTile] : make_float4(0.f, 0.f, 0.f, 0.f);
     return p;
   }
 
-  template <bool CHECK>
+  // CACHED: F and w come from the continuity pass (list entries of a step's momentum pass).
+  template <bool CHECK, bool CACHED = false>
   __device__ __forceinline__ bool geometry(uint32_t t, const Pre& p, df* d, df& r2, df& F, df& wv, df& mj) const {
     const float4 ah = p.ah, al = p.al;
     d[0] = df_sub_close(xi[0], df_make(ah.x, al.x));
@@ -339,19 +349,27 @@ struct DfPairs {
       }
     }
     if (!(r2.hi > 0.f)) return false;
-    const df inv_r = df_rsqrt(r2);
-    const df r = df_mul(r2, inv_r);
-    // F = c0 + c1 r + c2 / r on either piece of the spline, without a branch
-    const bool near = r.hi < w.h;
-    const df c0 = near ? df_make(w.near0[0], w.near0[1]) : df_make(w.far0[0], w.far0[1]);
-    const df c1 = near ? df_make(w.near1[0], w.near1[1]) : df_make(w.far1[0], w.far1[1]);
-    const df c2 = near ? df_make(0.f, 0.f) : df_make(w.far2[0], w.far2[1]);
-    F = df_add(df_add(c0, df_mul(c1, r)), df_mul(c2, inv_r));
-    const float4 bh = p.bh, bl = p.bl;
-    const df dv0 = df_sub(vi[0], df_make(bh.x, bl.x));
-    const df dv1 = df_sub(vi[1], df_make(bh.y, bl.y));
-    const df dv2 = DIM == 3 ? df_sub(vi[2], df_make(bh.z, bl.z)) : df_make(0.f, 0.f);
-    wv = df_dot3(dv0, dv1, dv2, d[0], d[1], d[2]);
+    if (CACHED) {
+      F = df_make(p.fw.x, p.fw.y);
+    } else {
+      const df inv_r = df_rsqrt(r2);
+      const df r = df_mul(r2, inv_r);
+      // F = c0 + c1 r + c2 / r on either piece of the spline, without a branch
+      const bool near = r.hi < w.h;
+      const df c0 = near ? df_make(w.near0[0], w.near0[1]) : df_make(w.far0[0], w.far0[1]);
+      const df c1 = near ? df_make(w.near1[0], w.near1[1]) : df_make(w.far1[0], w.far1[1]);
+      const df c2 = near ? df_make(0.f, 0.f) : df_make(w.far2[0], w.far2[1]);
+      F = df_add(df_add(c0, df_mul(c1, r)), df_mul(c2, inv_r));
+    }
+    if (CACHED) {
+      wv = df_make(p.fw.z, p.fw.w);
+    } else {
+      const float4 bh = p.bh, bl = p.bl;
+      const df dv0 = df_sub(vi[0], df_make(bh.x, bl.x));
+      const df dv1 = df_sub(vi[1], df_make(bh.y, bl.y));
+      const df dv2 = DIM == 3 ? df_sub(vi[2], df_make(bh.z, bl.z)) : df_make(0.f, 0.f);
+      wv = df_dot3(dv0, dv1, dv2, d[0], d[1], d[2]);
+    }
     mj = df_make(ah.w, al.w);
     return true;
   }
@@ -368,18 +386,22 @@ struct DfPairs {
     if (DIM == 3) dfacc_add_prod(acc[2], ncoef, d[2]);
   }
 
-  template <bool CHECK>
-  __device__ __forceinline__ void terms(uint32_t t, const Pre& p) {
+  template <bool CHECK, bool CACHED>
+  __device__ __forceinline__ void terms(uint32_t t, uint32_t q, const Pre& p) {
     df d[3], r2, F, wv, mj;
-    if (!geometry<CHECK>(t, p, d, r2, F, wv, mj)) return;
+    if (!geometry<CHECK, CACHED>(t, p, d, r2, F, wv, mj)) return;
+    if (STAGE == SPH_CONT && !CHECK && fc) fc[q * kListTile] = make_float4(F.hi, F.lo, wv.hi, wv.lo);
     if (kCont) dfacc_add_prod(dr, mj, df_mul(wv, F));
     if (kMom) momentum(p.rp, d, r2, F, wv, mj);
   }
 
-  // an entry of an exact neighbour list
-  __device__ __forceinline__ void pair_with(uint32_t t, const Pre& p) { terms<false>(t, p); }
-  // any candidate (the walk that continues an overflowed list)
-  __device__ __forceinline__ void pair(uint32_t t) { terms<true>(t, fetch(t)); }
+  // entry q of an exact neighbour list
+  __device__ __forceinline__ void pair_with(uint32_t t, uint32_t q, const Pre& p) {
+    if (STAGE == SPH_MOM && fc) terms<false, true>(t, q, p);
+    else terms<false, false>(t, q, p);
+  }
+  // any candidate (the walk that continues an overflowed list): everything computed here
+  __device__ __forceinline__ void pair(uint32_t t) { terms<true, false>(t, 0, fetch_entry(t, 0, false)); }
 
   __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id, uint32_t k) {
     const SphC<double>& c = K.d;

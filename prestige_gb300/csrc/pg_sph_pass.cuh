@@ -281,7 +281,8 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_kernel(SphArgs a, int
   }
 }
 
-// Policies that split a pair into fetch(t) (the neighbour's loads) and pair_with(t, fetched).
+// Policies that split a pair into fetch(t, q) (the loads for neighbour t, entry q of the list) and
+// pair_with(t, q, fetched).
 template <class P, class = void>
 struct PrefetchPolicy {
   static constexpr bool value = false;
@@ -316,12 +317,12 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_pass_kernel(SphArgs a
       // unrolled pair bodies (branch-free) interleave
       uint32_t t = L ? my[0] : k;
       uint32_t tn = L > 1 ? my[kListTile] : t;
-      typename Pairs::Pre cur = P.fetch(t);
+      typename Pairs::Pre cur = P.fetch(t, 0);
 #pragma unroll 2
       for (uint32_t q = 0; q < L; ++q) {
         const uint32_t tnn = q + 2 < L ? my[(q + 2) * kListTile] : tn;
-        const typename Pairs::Pre nxt = P.fetch(tn);
-        P.pair_with(t, cur);
+        const typename Pairs::Pre nxt = P.fetch(tn, q + 1 < L ? q + 1 : q);
+        P.pair_with(t, q, cur);
         cur = nxt;
         t = tn;
         tn = tnn;
