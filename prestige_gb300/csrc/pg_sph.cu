@@ -280,8 +280,8 @@ struct DfPairs {
   SphDF w;
   double four_h2;
   uint32_t kself;
-  float4* fc;  // per list entry {F.hi, F.lo, w.hi, w.lo}: written by the continuity pass, read by
-               // the momentum pass
+  float4* fc;  // per list entry {G.hi, G.lo, w.hi, w.lo} with G = m_j F: written by the continuity
+               // pass, read by the momentum pass
   df xi[3], vi[3], rhoi, Pi;
   dfacc acc[3], dr;
   static constexpr bool kCacheF = STAGE == SPH_CONT || STAGE == SPH_MOM;
@@ -332,7 +332,8 @@ struct DfPairs {
     return p;
   }
 
-  // CACHED: F and w come from the continuity pass (list entries of a step's momentum pass).
+  // CACHED: F holds G = m_j F and wv holds w, both from the continuity pass (list entries of a
+  // step's momentum pass).
   template <bool CHECK, bool CACHED = false>
   __device__ __forceinline__ bool geometry(uint32_t t, const Pre& p, df* d, df& r2, df& F, df& wv, df& mj) const {
     const float4 ah = p.ah, al = p.al;
@@ -374,13 +375,14 @@ struct DfPairs {
     return true;
   }
 
-  __device__ __forceinline__ void momentum(const float4& rpj, const df* d, df r2, df F, df wv, df mj) {
+  // G = m_j F (computed here, or from the cache)
+  __device__ __forceinline__ void momentum(const float4& rpj, const df* d, df r2, df G, df wv) {
     // artificial viscosity where the pair approaches (w < 0), computed for every pair and then
     // selected: nearly every warp has lanes on both sides
     const df den = df_mul(df_add(r2, df_make(w.eps_h2[0], w.eps_h2[1])), df_add(rhoi, df_make(rpj.x, rpj.y)));
     const df av = df_div(df_mul(df_make(w.avk[0], w.avk[1]), wv), den);
     const df pij = wv.hi < 0.f ? av : df_make(0.f, 0.f);
-    const df ncoef = df_neg(df_mul(mj, df_mul(df_add(df_add(Pi, df_make(rpj.z, rpj.w)), pij), F)));
+    const df ncoef = df_neg(df_mul(df_add(df_add(Pi, df_make(rpj.z, rpj.w)), pij), G));
     dfacc_add_prod(acc[0], ncoef, d[0]);
     dfacc_add_prod(acc[1], ncoef, d[1]);
     if (DIM == 3) dfacc_add_prod(acc[2], ncoef, d[2]);
@@ -390,9 +392,10 @@ struct DfPairs {
   __device__ __forceinline__ void terms(uint32_t t, uint32_t q, const Pre& p) {
     df d[3], r2, F, wv, mj;
     if (!geometry<CHECK, CACHED>(t, p, d, r2, F, wv, mj)) return;
-    if (STAGE == SPH_CONT && !CHECK && fc) fc[q * kListTile] = make_float4(F.hi, F.lo, wv.hi, wv.lo);
-    if (kCont) dfacc_add_prod(dr, mj, df_mul(wv, F));
-    if (kMom) momentum(p.rp, d, r2, F, wv, mj);
+    const df G = CACHED ? F : df_mul(mj, F);
+    if (STAGE == SPH_CONT && !CHECK && fc) fc[q * kListTile] = make_float4(G.hi, G.lo, wv.hi, wv.lo);
+    if (kCont) dfacc_add_prod(dr, G, wv);
+    if (kMom) momentum(p.rp, d, r2, G, wv);
   }
 
   // entry q of an exact neighbour list
