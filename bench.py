@@ -44,11 +44,13 @@ sys.path.insert(0, ROOT)
 MOM_BYTES = {"f64": 112, "f32": 56}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per particle of one momentum-pass
 # launch, from the ncu capture summarised in profiles/sph_step_df_lattice3d.md (1,000,000
-# particles, f64 double-word mode), scaled by the particle count.
-MOM_TRAFFIC_PER_PARTICLE = {"f64-fast": 511.0}
+# particles, f64 double-word mode), scaled by the particle count.  Most of it is the per-entry
+# cache the continuity pass writes for it (16 B per neighbour) and the neighbour lists (4 B per
+# neighbour): the pass reads cached pair terms instead of recomputing them.
+MOM_TRAFFIC_PER_PARTICLE = {"f64-fast": 1750.0}
 # The resource that binds the momentum pass in that capture: FMA-pipe cycles active (% of peak,
 # sm__pipe_fma_cycles_active) and issue slots active (smsp__issue_active).
-MOM_PIPES = {"f64-fast": {"fma_pipe_active_pct": 69.9, "issue_active_pct": 78.0}}
+MOM_PIPES = {"f64-fast": {"fma_pipe_active_pct": 54.1, "issue_active_pct": 69.1}}
 
 METRIC = "particle-steps/s"
 
@@ -341,7 +343,8 @@ def bench_dem(steps=30):
 
 def bench_sweep(steps=100, warmup=3, sizes=(262144, 1000000, 4096000)):
     """The 3D lattice sweep over N and arithmetic: device-timed steps (CUDA events on the
-    library's stream), block 256 and cell multiplier 0.5 for every case."""
+    library's stream), cell multiplier 0.5, the block size (64, 128 or 256) that ran a 3-step
+    trial fastest for the case, the arithmetic mode held fixed."""
     from prestige_gb300 import ParticleSystem, make_config, workloads
     cases = [("f64", 1, "double-word"), ("f64", 0, "IEEE"), ("f32", 1, "fast (FMA)"), ("f32", 0, "IEEE")]
     rows = []
@@ -350,7 +353,17 @@ def bench_sweep(steps=100, warmup=3, sizes=(262144, 1000000, 4096000)):
             w = workloads.sph_lattice_3d(n=n, seed=2, precision=1 if prec == "f64" else 0, f64_mode=mode)
             s = ParticleSystem(make_config(**w["config"]), w["n"])
             workloads.load_into(s, w)
-            s.set_tuning(256, 0.5, mode)
+            trials = {}
+            for block in (64, 128, 256):  # the trial steps advance the state; warm-up follows
+                s.set_tuning(block, 0.5, mode)
+                s.step(1)
+                s.timing_enable(True)
+                s.step_async(3)
+                s.sync()
+                trials[block] = s.timing_read()["region_ms"]
+                s.timing_enable(False)
+            best = min(trials, key=trials.get)
+            s.set_tuning(best, 0.5, mode)
             s.step(warmup)
             s.timing_enable(True)
             s.step_async(steps)
@@ -359,11 +372,11 @@ def bench_sweep(steps=100, warmup=3, sizes=(262144, 1000000, 4096000)):
             s.timing_enable(False)
             s.close()
             ms = t["region_ms"] / steps
-            rows.append({"particles": w["n"], "precision": prec, "arith": label, "ms_per_step": ms,
+            rows.append({"particles": w["n"], "precision": prec, "arith": label, "block": best, "ms_per_step": ms,
                          "value": w["n"] / (ms * 1e-3)})
     return {"workload": "jittered cubic lattice, dx=0.01, jitter +-0.2dx, h=1.3dx, v ~ N(0, 0.1), "
                         "rho = 1000(1 + U(-0.01, 0.01)), seed 2", "steps": steps, "unit": "particle-steps/s",
-            "tuning": "block 256, cell multiplier 0.5", "results": rows}
+            "tuning": "cell multiplier 0.5; block per case from a 3-step trial of 64, 128, 256", "results": rows}
 
 
 def run_gpu(args, rank, world, local, pgroup):
@@ -475,11 +488,12 @@ def run_gpu(args, rank, world, local, pgroup):
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "sph_list_pass_kernel (momentum pass)", "peak_source": peak_src,
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one momentum-pass "
-                                           "launch at 1,000,000 particles (511 B per particle), scaled by N"
+                                           "launch at 1,000,000 particles (1,750 B per particle: the per-entry cache and the lists), scaled by N"
                          if traffic else None,
                          "bytes_per_particle": bpp,
                          "pipes_ncu": MOM_PIPES.get("%s-%s" % (args.precision, args.mode)),
-                         "binding_resource": "FP32 issue (double-word f64 arithmetic)" if args.mode == "fast"
+                         "binding_resource": "FP32 issue (double-word f64 arithmetic) and the latency of the "
+                                             "per-entry cache and record loads" if args.mode == "fast"
                          and args.precision == "f64" else ("FP64 pipe" if args.precision == "f64" else "FP32 issue")},
             "stages_ms_per_step": {"neighbor_search": t["neighbor_ms"] / K, "sorted_gather": t["gather_ms"] / K,
                                    "neighbor_lists": list_ms, "continuity_pass": cont_ms, "momentum_pass": mom_ms},
