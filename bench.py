@@ -52,6 +52,15 @@ MOM_TRAFFIC_PER_PARTICLE = {"f64-fast": 1750.0}
 # sm__pipe_fma_cycles_active) and issue slots active (smsp__issue_active).
 MOM_PIPES = {"f64-fast": {"fma_pipe_active_pct": 54.1, "issue_active_pct": 69.1}}
 
+# Flops of the method (each +, -, *, / and sqrt of the oracle's f64 step one flop), counted by the
+# oracle's flop census on the 110,592-particle lattice of the same construction (seed 2):
+# per neighbour pair in each pass (position difference, r^2, spline, velocity term and, in the
+# momentum pass, viscosity where the pair approaches) and per particle (Tait pressure, density
+# update, velocity and position update).  tests/test_oracle_flops.py recomputes them.
+FLOPS_SAMPLE_PARTICLES = 110592
+FLOPS_PER_PAIR = {"continuity": 24.887, "momentum": 34.385}
+FLOPS_PER_PARTICLE = 28
+
 METRIC = "particle-steps/s"
 
 
@@ -401,6 +410,8 @@ def run_gpu(args, rank, world, local, pgroup):
     if not args.no_autotune:  # outside the timed region; the state is restored by the tuner
         tuning = s.autotune(trial_steps=2)
     info = s.info()
+    from prestige_gb300._native import measure_fma_peaks
+    fp64_peak, fp32_peak = measure_fma_peaks()  # ~10 ms of FMA chains, before the timed region
 
     # ---- device-timed steps, state resident in HBM ----
     s.step(args.warmup)
@@ -427,6 +438,13 @@ def run_gpu(args, rank, world, local, pgroup):
     peak, peak_src = _peak_hbm()
     tpp = MOM_TRAFFIC_PER_PARTICLE.get("%s-%s" % (args.precision, args.mode))
     traffic = tpp * n if tpp else None
+    # neighbour pairs per particle from the lists of the last timed step (lengths only)
+    pairs = float(s.pair_counts().mean())
+    exact_lists = args.precision == "f64" and args.mode == "fast"
+    flops_pp = pairs * (FLOPS_PER_PAIR["continuity"] + FLOPS_PER_PAIR["momentum"]) + FLOPS_PER_PARTICLE
+    flops_tf = flops_pp * n / (ms_per_step * 1e-3) / 1e12
+    pass_tf = pairs * (FLOPS_PER_PAIR["continuity"] + FLOPS_PER_PAIR["momentum"]) * n / \
+        ((cont_ms + mom_ms) * 1e-3) / 1e12
 
     # ---- end to end through the C ABI with pinned host buffers ----
     eb = 8 if args.precision == "f64" else 4
@@ -495,6 +513,20 @@ def run_gpu(args, rank, world, local, pgroup):
                          "binding_resource": "FP32 issue (double-word f64 arithmetic) and the latency of the "
                                              "per-entry cache and record loads" if args.mode == "fast"
                          and args.precision == "f64" else ("FP64 pipe" if args.precision == "f64" else "FP32 issue")},
+            "flops": {"per_particle_step": flops_pp, "pairs_per_particle": pairs,
+                      "pairs_source": "mean length of the exact neighbour lists of the last timed step"
+                      if exact_lists else "mean length of the FP32 superset lists (an upper bound)",
+                      "per_pair": FLOPS_PER_PAIR, "per_particle": FLOPS_PER_PARTICLE,
+                      "counted": "oracle flop census: each +, -, *, / and sqrt of the f64 step one flop; "
+                                 "candidate tests of non-neighbours excluded",
+                      "achieved_tflops": flops_tf, "pair_passes_tflops": pass_tf,
+                      "fp64_fma_peak_tflops": fp64_peak, "fp32_fma_peak_tflops": fp32_peak,
+                      "frac_fp64": flops_tf / fp64_peak, "frac_fp32": flops_tf / fp32_peak,
+                      "peak_source": "measured in this run: pg_measure_fma_peaks (8 independent FMA chains "
+                                     "per thread, 8 x 256 threads per SM)",
+                      "note": "f64 flops of the method; the double-word mode computes them on the FP32 pipe "
+                              "(several FP32 instructions per f64 flop), so frac_fp64 above 1 means the step runs "
+                              "its f64 arithmetic faster than the FP64 pipe could" if exact_lists else None},
             "stages_ms_per_step": {"neighbor_search": t["neighbor_ms"] / K, "sorted_gather": t["gather_ms"] / K,
                                    "neighbor_lists": list_ms, "continuity_pass": cont_ms, "momentum_pass": mom_ms},
             "stages_note": ("overlapped: neighbor_lists = lists of the first %d slots; continuity_pass = the "

@@ -251,6 +251,14 @@ int pg_autotune(pg_system* sys, int trial_steps, int* best_block, double* best_m
 /* Apply a tuning found earlier (e.g. cached by the host) without searching. */
 int pg_set_tuning(pg_system* sys, int block, double cell_multiplier, int f64_mode);
 
+/* Device characterisation: FP64 and FP32 FMA-pipe throughput of the current device in TFLOP/s
+ * (two flops per FMA), measured with eight independent FMA chains per thread, 8 blocks of 256
+ * threads per SM, timed with CUDA events after a warm-up launch (about 10 ms of GPU time).  These
+ * are the denominators of the pair passes' pipe fractions: the IEEE f64 passes run on the FP64
+ * pipe, the double-word and f32 passes on the FP32 pipe.  Either pointer may be NULL.  No
+ * reference counterpart. */
+int pg_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops);
+
 /* Device-side timing of steps (CUDA events on the handle's stream).  The momentum pass time is
  * pass_ms - list_ms - cont_ms.  pg_timing_enable(1) resets
  * the accumulators and makes every later step record events around its stages (steps then run

@@ -201,6 +201,22 @@ extern "C" double orc_sph_run(const orc_sph_spec* sp, int f64, long long n, void
   return run_t<float>(sp, (size_t)n, state, nsteps);
 }
 
+// Flop census of one SPH step on a double state (not modified), counted on one thread.
+// out: particles, candidates, pairs, continuity-loop flops, momentum-loop flops, step flops,
+// flops of one candidate test.
+extern "C" int orc_sph_flop_census(const orc_sph_spec* sp, long long n, void* const* state, double* out) {
+  SphSpec spec = to_spec(sp);
+  SphState<double> s;
+  load_state<double>(s, spec.dim, (size_t)n, (double* const*)state);
+  const int threads = omp_get_max_threads();
+  omp_set_num_threads(1);  // the flop counter is per thread
+  const SphFlopCensus c = spec.dim == 2 ? sph_flop_census<2>(spec, s) : sph_flop_census<3>(spec, s);
+  omp_set_num_threads(threads);
+  const double v[7] = {c.particles, c.candidates, c.pairs, c.cont_loops, c.mom_loops, c.step, c.test_flops};
+  for (int i = 0; i < 7; ++i) out[i] = v[i];
+  return 0;
+}
+
 // Forward-mode gradient of L = mean_i |x_i(T) - target_i|^2 over fluid particles after nsteps,
 // with respect to alpha, B and the initial velocities along direction u (3 dual components).
 // state: double arrays as orc_sph_run (not modified); u: dim arrays; target: dim arrays.

@@ -78,6 +78,29 @@ inline float prim(float x) { return x; }
 inline double prim(double x) { return x; }
 template <int K> inline double prim(const Dual<K>& x) { return x.v; }
 
+// A double that counts its arithmetic, for the flop census of a step (sph_flop_census).  Each
+// +, -, *, / and sqrt is one flop; negation, comparisons and conversions are free.  The count
+// is kept per thread: run counted code on one thread.
+inline uint64_t& flop_count() {
+  static thread_local uint64_t c = 0;
+  return c;
+}
+struct Counted {
+  double v;
+  Counted() : v(0.0) {}
+  Counted(double x) : v(x) {}
+};
+inline double value(const Counted& x) { return x.v; }
+inline double prim(const Counted& x) { return x.v; }
+template <> struct Prim<Counted> { typedef double type; };
+inline Counted operator+(const Counted& a, const Counted& b) { ++flop_count(); return Counted(a.v + b.v); }
+inline Counted operator-(const Counted& a, const Counted& b) { ++flop_count(); return Counted(a.v - b.v); }
+inline Counted operator*(const Counted& a, const Counted& b) { ++flop_count(); return Counted(a.v * b.v); }
+inline Counted operator/(const Counted& a, const Counted& b) { ++flop_count(); return Counted(a.v / b.v); }
+inline Counted operator-(const Counted& a) { return Counted(-a.v); }
+inline Counted sqrt(const Counted& a) { ++flop_count(); return Counted(std::sqrt(a.v)); }
+inline Counted fabs(const Counted& a) { return Counted(std::fabs(a.v)); }
+
 // ----------------------------------------------------------------------------------------
 // Cell grid.  Cell side s = mult * support * (1 + 2^-20); the tiny inflation keeps every
 // pair closer than `support` within `reach` cells of each other after rounding.
@@ -436,6 +459,60 @@ void sph_run(const SphSpec& spec, const SphConst<T>& k, SphState<T>& s, int nste
   cl.g = make_grid(DIM, spec.lo, spec.hi, 2.0 * spec.h, spec.cell_mult);
   std::vector<T> P;
   for (int it = 0; it < nsteps; ++it) sph_step<T, DIM>(spec, k, s, cl, P);
+}
+
+// Flop census of one SPH step (sph_step) on a state, counted with the Counted scalar on the
+// calling thread (run it with one OpenMP thread).  The pair loops are counted per particle, so
+// their totals split into candidate tests (d and r^2 of a candidate that is not a neighbour,
+// the particle itself included) and the pair terms of the neighbours (j != i within 2h).
+struct SphFlopCensus {
+  double particles = 0, candidates = 0, pairs = 0;
+  double cont_loops = 0, mom_loops = 0;  // flops of all continuity / momentum pair loops
+  double step = 0;                       // flops of the whole step (loops, Tait, updates)
+  double test_flops = 0;                 // flops of one candidate test (d and r^2)
+};
+
+template <int DIM>
+SphFlopCensus sph_flop_census(const SphSpec& spec, const SphState<double>& s0) {
+  SphState<Counted> s;
+  s.resize(s0.dim, s0.n);
+  for (size_t i = 0; i < s0.n; ++i) {
+    for (int c = 0; c < 3; ++c) { s.x[c][i] = s0.x[c][i]; s.v[c][i] = s0.v[c][i]; }
+    s.rho[i] = s0.rho[i];
+    s.m[i] = s0.m[i];
+  }
+  const SphConst<Counted> k = sph_consts<Counted>(spec, Counted(spec.alpha), Counted(spec.B));
+  SphFlopCensus out;
+  out.particles = (double)s.n;
+  out.test_flops = 3 * DIM - 1;
+  CellList cl;
+  cl.g = make_grid(DIM, spec.lo, spec.hi, 2.0 * spec.h, spec.cell_mult);
+  const Counted* pos[3] = {s.x[0].data(), s.x[1].data(), DIM == 3 ? s.x[2].data() : s.x[0].data()};
+  build_cell_list<Counted>(cl, s.n, pos);
+  std::vector<Counted> P(s.n);
+  for (size_t i = 0; i < s.n; ++i) P[i] = tait_pterm(k, s.rho[i]);
+  for (size_t i = 0; i < s.n; ++i) {
+    for_each_candidate(cl, cl.cell[i], [&](uint32_t j) {
+      double d[3];
+      for (int c = 0; c < DIM; ++c) d[c] = s.x[c][i].v - s.x[c][j].v;
+      const double r2 = dist2<double, DIM>(d);
+      out.candidates += 1;
+      if (r2 < k.four_h2.v && r2 > 0.0) out.pairs += 1;
+    });
+    Counted a[3], dr;
+    flop_count() = 0;
+    sph_pair_loop<Counted, DIM, true, false>(cl, s, k, P, i, a, dr);
+    out.cont_loops += (double)flop_count();
+    flop_count() = 0;
+    sph_pair_loop<Counted, DIM, false, true>(cl, s, k, P, i, a, dr);
+    out.mom_loops += (double)flop_count();
+  }
+  std::vector<Counted> Pstep;
+  flop_count() = 0;
+  sph_step<Counted, DIM>(spec, k, s, cl, Pstep);
+  out.step = (double)flop_count();
+  flop_count() = 0;
+  return out;
 }
 
 // ----------------------------------------------------------------------------------------

@@ -202,6 +202,20 @@ def sph_run(cfg, state, nsteps):
                               int(nsteps))
 
 
+def sph_flop_census(cfg, state):
+    """Counted flops of one oracle SPH step on `state` (f64, not modified): a dict with the
+    particle, candidate and neighbour-pair counts, the flops of the continuity and momentum pair
+    loops, of the whole step, and of one candidate test (d and r^2).  Each +, -, *, / and sqrt
+    counts one flop."""
+    assert state.f64
+    spec = sph_spec(cfg, state.n)
+    out = np.zeros(7)
+    load().orc_sph_flop_census(ctypes.byref(spec), ctypes.c_longlong(state.n), state.ptrs(),
+                               out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    keys = ("particles", "candidates", "pairs", "cont_loops", "mom_loops", "step", "test_flops")
+    return dict(zip(keys, out.tolist()))
+
+
 def sph_grad_dual(cfg, state, u, target, nsteps):
     """Forward-mode (dual number) L, dL/dalpha, dL/dB, <dL/dv0, u> with
     L = mean over fluid particles of |x(T) - target|^2."""

@@ -93,6 +93,7 @@ SIGNATURES = {
     "pg_autotune": (_I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I),
                          ctypes.POINTER(ctypes.c_double)]),
     "pg_set_tuning": (_I, [_P, _I, ctypes.c_double, _I]),
+    "pg_measure_fma_peaks": (_I, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "pg_timing_enable": (_I, [_P, _I]),
     "pg_timing_read": (_I, [_P, ctypes.POINTER(PgTiming)]),
     "pg_memory_bytes": (_I, [_P, ctypes.POINTER(_SZ)]),
@@ -145,3 +146,10 @@ def default_config():
     c = PgConfig()
     load().pg_config_default(ctypes.byref(c))
     return c
+
+
+def measure_fma_peaks():
+    """(fp64, fp32) FMA-pipe throughput of the current device in TFLOP/s (pg_measure_fma_peaks)."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    check(load().pg_measure_fma_peaks(ctypes.byref(a), ctypes.byref(b)), "pg_measure_fma_peaks")
+    return a.value, b.value

@@ -102,10 +102,85 @@ int time_steps(pg_system* s, int steps, double* ms) {
   return st;
 }
 
+// Independent FMA chains, eight per thread: throughput of the FMA pipe of type T.
+template <class T>
+__device__ __forceinline__ T fma_rn(T a, T b, T c);
+template <>
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+template <>
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+constexpr int kChains = 8;
+
+template <class T>
+__global__ void fma_chains_kernel(T* out, int iters, T a, T b) {
+  T acc[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) acc[c] = (T)(threadIdx.x + c);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) acc[c] = fma_rn<T>(acc[c], a, b);
+  }
+  T sum = 0;
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) sum += acc[c];
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = sum;
+}
+
+// TFLOP/s of the chains (two flops per FMA), timed with events after one warm-up launch.
+template <class T>
+int time_fma_chains(cudaStream_t st, void* out, int blocks, int threads, int iters, double* tflops) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  PG_CUDA_TRY(cudaEventCreate(&e0));
+  PG_CUDA_TRY(cudaEventCreate(&e1));
+  fma_chains_kernel<T><<<blocks, threads, 0, st>>>((T*)out, iters / 10, (T)0.999, (T)1e-3);
+  cudaEventRecord(e0, st);
+  fma_chains_kernel<T><<<blocks, threads, 0, st>>>((T*)out, iters, (T)0.999, (T)1e-3);
+  cudaEventRecord(e1, st);
+  cudaError_t err = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (err != cudaSuccess) {
+    set_error("FMA chains: %s", cudaGetErrorString(err));
+    return PG_ECUDA;
+  }
+  *tflops = 2.0 * kChains * (double)iters * blocks * threads / (ms * 1e-3) / 1e12;
+  return PG_OK;
+}
+
 }  // namespace
 }  // namespace pg
 
 extern "C" {
+
+int pg_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops) {
+  pg::clear_error();
+  int dev = 0, sms = 0;
+  PG_CUDA_TRY(cudaGetDevice(&dev));
+  PG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = sms * 8, threads = 256;
+  cudaStream_t st = nullptr;
+  PG_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  void* out = nullptr;
+  cudaError_t err = cudaMalloc(&out, (size_t)blocks * threads * sizeof(double));
+  if (err != cudaSuccess) {
+    cudaStreamDestroy(st);
+    pg::set_error("cudaMalloc: %s", cudaGetErrorString(err));
+    return PG_ECUDA;
+  }
+  double t64 = 0.0, t32 = 0.0;
+  int rc = pg::time_fma_chains<double>(st, out, blocks, threads, 2000, &t64);
+  if (rc == PG_OK) rc = pg::time_fma_chains<float>(st, out, blocks, threads, 20000, &t32);
+  cudaFree(out);
+  cudaStreamDestroy(st);
+  if (rc != PG_OK) return rc;
+  if (fp64_tflops) *fp64_tflops = t64;
+  if (fp32_tflops) *fp32_tflops = t32;
+  return PG_OK;
+}
+
 
 int pg_set_tuning(pg_system* s, int block, double cell_multiplier, int f64_mode) {
   pg::clear_error();

@@ -194,6 +194,14 @@ class ParticleSystem:
                   "pg_get_pair_lists")
         return lengths, entries
 
+    def pair_counts(self):
+        """Lengths of the pair-pass neighbour lists built by the last step or compute_rates, per
+        sorted slot (exact neighbour counts, the particle itself excluded, in the f64
+        double-word mode; FP32 superset counts otherwise)."""
+        lengths = np.empty(self.n, np.uint32)
+        nat.check(self._lib.pg_get_pair_lists(self._h, lengths.ctypes.data, None, 0), "pg_get_pair_lists")
+        return lengths
+
     def run_equations(self, bodies):
         """Run fused pairwise equation bodies (source text) on the GPU over the neighbour set."""
         if isinstance(bodies, str):

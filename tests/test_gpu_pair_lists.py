@@ -157,3 +157,25 @@ def test_overflowed_lists_report_full_lengths(pg, oracle):
         assert lengths[k] == len(r)
         m = min(len(r), 20)
         assert np.array_equal(ids[entries[k, :m]], r[:m])
+
+
+def test_pair_counts_are_the_oracle_pair_count(pg, oracle):
+    """The list lengths of the double-word mode sum to the oracle's neighbour-pair count (j != i
+    within 2h), the figure bench.py multiplies by the per-pair flops."""
+    from oracle import py_oracle as po
+    w = workloads.sph_lattice_3d(n=4096, seed=2)
+    s, cfg = _system(w, 1)
+    s.compute_rates()
+    counts = s.pair_counts()
+    lengths, _ = s.pair_lists()
+    assert np.array_equal(counts, lengths)
+    f = w["fields"]
+    census = po.sph_flop_census(cfg, po.SphState(f["pos"], f["vel"], f["rho"], f["mass"]))
+    assert int(counts.sum()) == int(census["pairs"])
+
+
+def test_measure_fma_peaks(pg):
+    from prestige_gb300._native import measure_fma_peaks
+    fp64, fp32 = measure_fma_peaks()
+    assert np.isfinite(fp64) and np.isfinite(fp32)
+    assert 0.0 < fp64 < fp32
