@@ -18,8 +18,16 @@
 //                     pair terms needs (errors relative to the sum of magnitudes)
 //   df_mul            "DWTimesDW3" (Joldes, Muller & Popescu 2017, Alg. 12), rel. error <= 4u^2
 //   df_mul_f          "DWTimesFP3" (ibid., Alg. 9), rel. error <= 2u^2
-//   df_div            one Newton/Karp-Markstein correction of q1 = x.hi * (1/y.hi) using the
-//                     double-word remainder x - q1*y (Karp & Markstein 1997)
+//   df_add_raw        df_add without its final Fast2Sum: the same value, with a lo part of up to
+//                     about 2^-24 (|x| + |y|), more than ulp(hi)/2 where x and y cancel.  For
+//                     operands of products and dot products (df_mul, df_mul_f, df_div, df_dot3,
+//                     dfacc_add_prod), which take hi into an error-free transform and lo into an
+//                     FP32 correction term: the rounding of that term, 2^-24 |lo| times the other
+//                     factor, stays within the sum's own error bound (~2u^2 (|x| + |y|)) times it
+//   df_div            one Newton/Karp-Markstein correction of q1 = x.hi * t, t the hardware
+//                     approximate reciprocal of y.hi (rcp.approx, relative error below 2^-23), using
+//                     the double-word remainder x - q1*y (Karp & Markstein 1997): the correction
+//                     leaves a relative error of about t's error squared, below 2^-44
 //   df_rsqrt          one Newton correction of the FP32 reciprocal square root, with the
 //                     residual 1 - a*y^2 formed in double-word arithmetic
 //   df_sumsq3 /       |x|^2 and x.y of 3-vectors: the three hi products by TwoProd, summed by
@@ -142,6 +150,21 @@ __device__ __forceinline__ df df_add(df x, df y) {
 
 __device__ __forceinline__ df df_sub(df x, df y) { return df_add(x, df_neg(y)); }
 
+__device__ __forceinline__ df df_add_raw(df x, df y) {
+  const df s = two_sum(x.hi, y.hi);
+  return df_make(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+
+__device__ __forceinline__ df df_sub_raw(df x, df y) { return df_add_raw(x, df_neg(y)); }
+
+// Approximate reciprocal (PTX rcp.approx.ftz.f32: relative error below 2^-23, subnormals
+// flushed); the seed of df_div, whose correction step makes up the difference.
+__device__ __forceinline__ float rcp_approx(float y) {
+  float t;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(t) : "f"(y));
+  return t;
+}
+
 // x - y when the hi parts lie within a factor 2 of each other, so that their difference is exact
 // (Sterbenz 1974): 5 operations in place of 11.  Fast2Sum applies because a nonzero hi
 // difference is at least one ulp of the operands and each lo part is at most half of one.
@@ -167,8 +190,9 @@ __device__ __forceinline__ df df_mul_f(df x, float y) {
   return fast_two_sum(c.hi, __fmaf_rn(x.lo, y, c.lo));
 }
 
+// y.hi must be a normal float (the divisors here are densities and squared distances).
 __device__ __forceinline__ df df_div(df x, df y) {
-  const float t = __frcp_rn(y.hi);
+  const float t = rcp_approx(y.hi);
   const float q1 = __fmul_rn(x.hi, t);
   const df r = df_sub(x, df_mul_f(y, q1));
   const float q2 = __fmul_rn(r.hi, t);

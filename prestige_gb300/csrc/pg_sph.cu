@@ -360,15 +360,16 @@ struct DfPairs {
       const df c0 = near ? df_make(w.near0[0], w.near0[1]) : df_make(w.far0[0], w.far0[1]);
       const df c1 = near ? df_make(w.near1[0], w.near1[1]) : df_make(w.far1[0], w.far1[1]);
       const df c2 = near ? df_make(0.f, 0.f) : df_make(w.far2[0], w.far2[1]);
-      F = df_add(df_add(c0, df_mul(c1, r)), df_mul(c2, inv_r));
+      F = df_add_raw(df_add_raw(c0, df_mul(c1, r)), df_mul(c2, inv_r));  // consumed by products
     }
     if (CACHED) {
       wv = df_make(p.fw.z, p.fw.w);
     } else {
       const float4 bh = p.bh, bl = p.bl;
-      const df dv0 = df_sub(vi[0], df_make(bh.x, bl.x));
-      const df dv1 = df_sub(vi[1], df_make(bh.y, bl.y));
-      const df dv2 = DIM == 3 ? df_sub(vi[2], df_make(bh.z, bl.z)) : df_make(0.f, 0.f);
+      // velocity differences, consumed by the dot product only
+      const df dv0 = df_sub_raw(vi[0], df_make(bh.x, bl.x));
+      const df dv1 = df_sub_raw(vi[1], df_make(bh.y, bl.y));
+      const df dv2 = DIM == 3 ? df_sub_raw(vi[2], df_make(bh.z, bl.z)) : df_make(0.f, 0.f);
       wv = df_dot3(dv0, dv1, dv2, d[0], d[1], d[2]);
     }
     mj = df_make(ah.w, al.w);
@@ -379,10 +380,11 @@ struct DfPairs {
   __device__ __forceinline__ void momentum(const float4& rpj, const df* d, df r2, df G, df wv) {
     // artificial viscosity where the pair approaches (w < 0), computed for every pair and then
     // selected: nearly every warp has lanes on both sides
-    const df den = df_mul(df_add(r2, df_make(w.eps_h2[0], w.eps_h2[1])), df_add(rhoi, df_make(rpj.x, rpj.y)));
+    // two sums of positive terms, consumed by the product only
+    const df den = df_mul(df_add_raw(r2, df_make(w.eps_h2[0], w.eps_h2[1])), df_add_raw(rhoi, df_make(rpj.x, rpj.y)));
     const df av = df_div(df_mul(df_make(w.avk[0], w.avk[1]), wv), den);
     const df pij = wv.hi < 0.f ? av : df_make(0.f, 0.f);
-    const df ncoef = df_neg(df_mul(df_add(df_add(Pi, df_make(rpj.z, rpj.w)), pij), G));
+    const df ncoef = df_neg(df_mul(df_add_raw(df_add_raw(Pi, df_make(rpj.z, rpj.w)), pij), G));
     dfacc_add_prod(acc[0], ncoef, d[0]);
     dfacc_add_prod(acc[1], ncoef, d[1]);
     if (DIM == 3) dfacc_add_prod(acc[2], ncoef, d[2]);

@@ -9,6 +9,10 @@
 //   df_sub_close    exact hi difference: when the hi parts are within a factor 2, hi + lo equals
 //                   the difference of the operands to within one rounding of the lo difference
 //                   (2^-46 of the operands' magnitude)
+//   df_div          quotient of double-word operands within 2^-43 of the f64 quotient of their
+//                   values (the approximate-reciprocal seed plus one correction)
+//   df_add_raw      the value of df_add (within 2^-46 of |x| + |y|), its lo part at most
+//                   2^-23 (|hi| + |x| + |y|)
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -38,6 +42,23 @@ __global__ void sub_kernel(const double* a, const double* b, int n, double* exac
   // the f64 value of the double-word difference of the double-words (exact in f64)
   exact[i] = __dsub_rn(__dadd_rn((double)ah, (double)al), __dadd_rn((double)bh, (double)bl));
   got[i] = __dadd_rn((double)d.hi, (double)d.lo);
+}
+
+__global__ void div_add_kernel(const double* a, const double* b, int n, double* q, double* sn, double* sr,
+                               float* rhi, float* rlo) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float ah, al, bh, bl;
+  df_split(a[i], &ah, &al);
+  df_split(b[i], &bh, &bl);
+  const df x = df_make(ah, al), y = df_make(bh, bl);
+  const df d = df_div(x, y);
+  q[i] = __dadd_rn((double)d.hi, (double)d.lo);
+  const df s = df_add(x, y), r = df_add_raw(x, y);
+  sn[i] = __dadd_rn((double)s.hi, (double)s.lo);
+  sr[i] = __dadd_rn((double)r.hi, (double)r.lo);
+  rhi[i] = r.hi;
+  rlo[i] = r.lo;
 }
 
 static double from_bits(uint64_t b) {
@@ -128,6 +149,54 @@ int main() {
       if (bad_sub < 10) std::fprintf(stderr, "sub %.17g - %.17g: %.17g vs %.17g\n", A[i], B[i], G[i], E[i]);
       ++bad_sub;
     }
-  std::printf("arith_check: %d values, %d split mismatches; %d differences, %d out of bound\n", n, bad, m, bad_sub);
-  return bad || bad_sub ? 1 : 0;
+  // df_div and df_add_raw on operands over 12 decades, both signs
+  std::vector<double> X(m), Y(m);
+  std::uniform_real_distribution<double> Dec(-6.0, 6.0), S(0.0, 1.0);
+  for (int i = 0; i < m; ++i) {
+    X[i] = std::pow(10.0, Dec(rng)) * (S(rng) < 0.5 ? -1.0 : 1.0);
+    Y[i] = std::pow(10.0, Dec(rng)) * (S(rng) < 0.5 ? -1.0 : 1.0);
+  }
+  double *dq, *dsn, *dsr;
+  float *drh, *drl;
+  cudaMalloc(&dq, 8 * m);
+  cudaMalloc(&dsn, 8 * m);
+  cudaMalloc(&dsr, 8 * m);
+  cudaMalloc(&drh, 4 * m);
+  cudaMalloc(&drl, 4 * m);
+  cudaMemcpy(da, X.data(), 8 * m, cudaMemcpyHostToDevice);
+  cudaMemcpy(db, Y.data(), 8 * m, cudaMemcpyHostToDevice);
+  div_add_kernel<<<(m + 255) / 256, 256>>>(da, db, m, dq, dsn, dsr, drh, drl);
+  std::vector<double> Q(m), SN(m), SR(m);
+  std::vector<float> RH(m), RL(m);
+  cudaMemcpy(Q.data(), dq, 8 * m, cudaMemcpyDeviceToHost);
+  cudaMemcpy(SN.data(), dsn, 8 * m, cudaMemcpyDeviceToHost);
+  cudaMemcpy(SR.data(), dsr, 8 * m, cudaMemcpyDeviceToHost);
+  cudaMemcpy(RH.data(), drh, 4 * m, cudaMemcpyDeviceToHost);
+  cudaMemcpy(RL.data(), drl, 4 * m, cudaMemcpyDeviceToHost);
+  if (cudaGetLastError() != cudaSuccess) {
+    std::fprintf(stderr, "CUDA error\n");
+    return 2;
+  }
+  int bad_div = 0, bad_add = 0;
+  for (int i = 0; i < m; ++i) {
+    float xh, xl, yh, yl;
+    df_split(X[i], &xh, &xl);
+    df_split(Y[i], &yh, &yl);
+    const double xv = (double)xh + (double)xl, yv = (double)yh + (double)yl;
+    const double qref = xv / yv;
+    if (!(std::fabs(Q[i] - qref) <= std::ldexp(std::fabs(qref), -43))) {
+      if (bad_div < 10) std::fprintf(stderr, "div %.17g / %.17g: %.17g vs %.17g\n", xv, yv, Q[i], qref);
+      ++bad_div;
+    }
+    const double scale = std::fabs(xv) + std::fabs(yv);
+    const bool val_ok = std::fabs(SR[i] - SN[i]) <= std::ldexp(scale, -46);
+    const bool lo_ok = std::fabs((double)RL[i]) <= std::ldexp(std::fabs((double)RH[i]) + scale, -23);
+    if (!val_ok || !lo_ok) {
+      if (bad_add < 10) std::fprintf(stderr, "add_raw %.17g + %.17g: %.17g vs %.17g (lo %a hi %a)\n", xv, yv, SR[i], SN[i], RL[i], RH[i]);
+      ++bad_add;
+    }
+  }
+  std::printf("arith_check: %d values, %d split mismatches; %d differences, %d out of bound; %d quotients, %d out of "
+              "bound; %d raw sums, %d out of bound\n", n, bad, m, bad_sub, m, bad_div, m, bad_add);
+  return bad || bad_sub || bad_div || bad_add ? 1 : 0;
 }
