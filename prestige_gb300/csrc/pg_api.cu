@@ -428,7 +428,8 @@ int capture_graphs(pg_system* s) {
       set_error("graph capture failed: %s", cudaGetErrorString(ce));
       return PG_ECUDA;
     }
-    cudaError_t ie = cudaGraphInstantiate(&s->graph_exec[gi], graph, 0);
+    // node priorities: the overlapped step's list kernel keeps its stream's priority in a graph
+    cudaError_t ie = cudaGraphInstantiate(&s->graph_exec[gi], graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
     if (ie != cudaSuccess) {
       s->hcur = hsave;
@@ -442,11 +443,14 @@ int capture_graphs(pg_system* s) {
 
 // Overlap of the continuity pass (FMA-bound) with the list kernel (ALU-bound) for double-word
 // SPH handles of at least 1M particles: the lists of the first 70 % of the slots are built
-// first, then the continuity pass over them runs beside the lists of the rest.  The two
-// kernels' persistent grids are sized so that their blocks fit on an SM together (two thirds of
-// the pass's blocks, registers per block from the kernels' attributes).  Measured at 4M
-// particles: 9.27 ms per step against 9.46 without the overlap; splits of 0.35 and 0.5 and a
-// single pass block per SM were slower.  At 1M particles it is even (2.37 against 2.40 ms), at
+// first, then the continuity pass over them runs beside the lists of the rest.  The list
+// kernel's persistent grid leaves room on every SM for two thirds of the pass's blocks
+// (registers per block from the kernels' attributes) and runs on a stream of the highest
+// priority, so its blocks are placed first; the continuity pass runs one block per tile and
+// fills the SMs as the list blocks finish.  Measured at 4M particles: 9.27 ms per step against
+// 9.46 without the overlap, with both kernels on persistent grids; 7.76 against 8.10 ms with
+// the backfilling pass and the priority (8.11 with the backfilling pass alone); splits of 0.35
+// and 0.5 and a single pass block per SM were slower with persistent grids.  At 1M particles it is even (2.37 against 2.40 ms), at
 // 256k slower (0.81 against 0.75 ms), hence the threshold; the 512-system batch of 2D dam
 // breaks (6.1M particles) was slower with it too (3.91 against 3.81 ms), so batched handles
 // keep the sequential schedule.
@@ -461,10 +465,16 @@ int choose_overlap(pg_system* s, int sms) {
   int bl = (regs - bp * per_block_p) / per_block_l;
   bl = std::min(bl, (threads - bp * s->block) / s->block);
   if (bl < 1) return PG_OK;
-  if (!s->aux) PG_CUDA_TRY(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
+  if (!s->aux) {  // the list kernel's blocks are placed first, the continuity pass fills the rest
+    int least = 0, greatest = 0;
+    PG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    PG_CUDA_TRY(cudaStreamCreateWithPriority(&s->aux, cudaStreamNonBlocking, greatest));
+  }
   for (int i = 0; i < 2; ++i)
     if (!s->ov_ev[i]) PG_CUDA_TRY(cudaEventCreateWithFlags(&s->ov_ev[i], cudaEventDisableTiming));
-  s->ov_pass_grid = bp * sms;
+  // the continuity pass beside the lists runs one block per tile, so the block scheduler fills
+  // the SMs with it as the list kernel's blocks finish
+  s->ov_pass_grid = 0;
   s->ov_list_grid = bl * sms;
   s->ov_split = (uint32_t)(s->n * 7 / 10 / (size_t)s->block * (size_t)s->block);
   return PG_OK;
