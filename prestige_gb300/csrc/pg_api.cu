@@ -233,7 +233,9 @@ int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[2], s->stream));
   if (!rates && s->ov_split > 0 && s->ov_split < s->n) {
     // lists of [0, split) first; then the continuity pass over them runs beside the lists of
-    // [split, n) on the auxiliary stream; the momentum pass needs every rho', so it runs last
+    // [split, n) on the auxiliary stream, which goes on with the continuity pass over
+    // [split, n) (neither continuity launch reads the packed rho' the other writes); the
+    // momentum pass needs every rho', so it runs last
     SphArgs a1 = a, a2 = a;
     a1.k_end = s->ov_split;
     a2.k_begin = s->ov_split;
@@ -243,10 +245,10 @@ int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
     PG_CUDA_TRY(cudaEventRecord(s->ov_ev[0], s->stream));
     PG_CUDA_TRY(cudaStreamWaitEvent(s->aux, s->ov_ev[0], 0));
     PG_TRY(launch_sph_list(s->aux, a2, s->arith, s->ov_list_grid, s->block));
+    PG_TRY(launch_sph_list_pass(s->aux, a2, s->arith, SPH_CONT, 0, s->block));  // one block per tile
     PG_CUDA_TRY(cudaEventRecord(s->ov_ev[1], s->aux));
     PG_TRY(launch_sph_list_pass(s->stream, a1, s->arith, SPH_CONT, s->ov_pass_grid, s->block));
     PG_CUDA_TRY(cudaStreamWaitEvent(s->stream, s->ov_ev[1], 0));
-    PG_TRY(launch_sph_list_pass(s->stream, a2, s->arith, SPH_CONT, s->pass_grid[SPH_CONT], s->block));
     if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
     PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], s->block));
     s->launches += neighbor_launches(s) + 6;
@@ -443,20 +445,24 @@ int capture_graphs(pg_system* s) {
 
 // Overlap of the continuity pass (FMA-bound) with the list kernel (ALU-bound) for double-word
 // SPH handles of at least 1M particles: the lists of the first 70 % of the slots are built
-// first, then the continuity pass over them runs beside the lists of the rest.  The list
-// kernel's persistent grid leaves room on every SM for two thirds of the pass's blocks
-// (registers per block from the kernels' attributes) and runs on a stream of the highest
-// priority, so its blocks are placed first; the continuity pass runs one block per tile and
-// fills the SMs as the list blocks finish.  Measured at 4M particles: 9.27 ms per step against
-// 9.46 without the overlap, with both kernels on persistent grids; 7.76 against 8.10 ms with
-// the backfilling pass and the priority (8.11 with the backfilling pass alone); splits of 0.35
-// and 0.5 and a single pass block per SM were slower with persistent grids.  At 1M particles it is even (2.37 against 2.40 ms), at
-// 256k slower (0.81 against 0.75 ms), hence the threshold; the 512-system batch of 2D dam
-// breaks (6.1M particles) was slower with it too (3.91 against 3.81 ms), so batched handles
-// keep the sequential schedule.
+// first, then the continuity pass over them runs beside the lists of the rest, and the
+// continuity pass over the rest follows those lists on their stream.  The list kernel's
+// persistent grid leaves room on every SM for two thirds of the pass's blocks (registers per
+// block from the kernels' attributes) and runs on a stream of the highest priority, so its
+// blocks are placed first; the continuity passes run one block per tile and fill the SMs as the
+// list blocks finish.  Measured at 4M particles (ms per step):
+//   no overlap, persistent grids                                          9.46
+//   overlap with both kernels on persistent grids                        9.27
+//   the same build later: persistent grids 8.10, backfilling pass 8.11,
+//   backfilling pass and list-stream priority 7.76
+//   continuity over the rest on the list stream                           7.65 (7.70 without)
+//   splits 0.5 / 0.6 / 0.8 of the slots                                   7.92 / 7.72 / 7.69
+// At 1M particles it is even (1.965 ms either way), at 256k slower (0.690 against 0.670 ms),
+// hence the threshold.  The 512-system batch of 2D dam breaks (6.1M particles, one handle)
+// gains too: 3.36 against 3.45 ms (with persistent grids it had lost, 3.91 against 3.81).
 int choose_overlap(pg_system* s, int sms) {
   s->ov_split = 0;
-  if (s->model != PG_MODEL_SPH || s->arith != ARITH_F64_DF || s->n < 1000000 || s->nsys > 1) return PG_OK;
+  if (s->model != PG_MODEL_SPH || s->arith != ARITH_F64_DF || s->n < 1000000) return PG_OK;
   const int rp = sph_list_regs(s->arith, s->dim, SPH_CONT), rl = sph_list_regs(s->arith, s->dim, -1);
   if (rp <= 0 || rl <= 0) return PG_OK;
   const int per_block_p = ((rp + 7) / 8) * 8 * s->block, per_block_l = ((rl + 7) / 8) * 8 * s->block;

@@ -86,3 +86,27 @@ def test_batch_of_one_equals_plain_handle(pg):
     s.step(4)
     assert np.array_equal(b.get("pos"), s.get("pos"))
     assert np.array_equal(b.get("rho"), s.get("rho"))
+
+
+def test_batch_overlapped_step_within_tolerance(pg, oracle):
+    """A double-word batch of more than 1M particles takes the overlapped schedule (lists of
+    the first slots, continuity passes beside the rest of the lists on a second stream); the
+    split falls inside a system.  Every system stays within the f64 tolerance of its oracle run."""
+    systems = workloads.batched_dam_breaks(n_systems=40, nmin=20000, nmax=40000, seed=12)
+    assert sum(w["n"] for w in systems) >= 1000000
+    b = _batch(systems, 1)
+    split = b.info()["overlap_split"]
+    assert 0 < split < b.n
+    bounds = np.cumsum([0] + [w["n"] for w in systems])
+    assert not np.isin(split, bounds)  # the split is inside a system
+    nsteps = 2
+    b.step(nsteps)
+    ref = _oracle_runs(oracle, systems, nsteps)
+    pos, rho = b.get("pos"), b.get("rho")
+    o = 0
+    for w, st in zip(systems, ref):
+        n = w["n"]
+        assert np.abs(pos[o:o + n] - st.pos).max() <= F64_TOL * np.abs(st.pos).max()
+        assert np.abs(rho[o:o + n] - st.rho).max() <= F64_TOL * np.abs(st.rho).max()
+        o += n
+    b.close()
