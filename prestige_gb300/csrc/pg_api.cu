@@ -457,6 +457,10 @@ int capture_graphs(pg_system* s) {
 //   backfilling pass and list-stream priority 7.76
 //   continuity over the rest on the list stream                           7.65 (7.70 without)
 //   splits 0.5 / 0.6 / 0.8 of the slots                                   7.92 / 7.72 / 7.69
+// A finer pipeline (the slots in 4, 8 or 16 even chunks, each chunk's continuity pass starting
+// when its lists are done) gave 7.80 / 7.84 / 8.02 ms against 7.76 for two chunks on the same
+// box: lists and continuity add up to about 4.4 ms however they are interleaved, so once the SMs
+// are backfilled the two kernels share a saturated machine.
 // At 1M particles it is even (1.965 ms either way), at 256k slower (0.690 against 0.670 ms),
 // hence the threshold.  The 512-system batch of 2D dam breaks (6.1M particles, one handle)
 // gains too: 3.36 against 3.45 ms (with persistent grids it had lost, 3.91 against 3.81).
