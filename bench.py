@@ -79,6 +79,10 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the batched, adjoint and DEM sections")
     p.add_argument("--no-autotune", action="store_true", help="keep the default block size and cell multiplier")
+    p.add_argument("--block", type=int, default=0,
+                   help="fixed block size of the list kernels instead of the autotuner's (with --cell-mult)")
+    p.add_argument("--cell-mult", type=float, default=0.5, help="cell multiplier used with --block")
+    p.add_argument("--mom-block", type=int, default=0, help="momentum-pass block size used with --block (0: --block)")
     p.add_argument("--section", default="all", choices=["all", "batched", "adjoint", "dem", "sweep"],
                    help="run only one extra section and print its JSON (for profiling)")
     p.add_argument("--adjoint-steps", type=int, default=500)
@@ -407,8 +411,13 @@ def run_gpu(args, rank, world, local, pgroup):
     s = ParticleSystem(make_config(**w["config"]), n)
     workloads.load_into(s, w)
     tuning = None
-    if not args.no_autotune:  # outside the timed region; the state is restored by the tuner
-        tuning = s.autotune(trial_steps=2)
+    if args.block:
+        s.set_tuning(args.block, args.cell_mult, 1 if args.mode == "fast" else 0)
+        s.set_momentum_block(args.mom_block)
+        tuning = {"block_size": args.block, "momentum_block": s.info()["momentum_block"],
+                  "cell_multiplier": args.cell_mult, "fixed": True}
+    elif not args.no_autotune:  # outside the timed region; the state is restored by the tuner
+        tuning = s.autotune(trial_steps=3)
     info = s.info()
     from prestige_gb300._native import measure_fma_peaks
     fp64_peak, fp32_peak = measure_fma_peaks()  # ~10 ms of FMA chains, before the timed region

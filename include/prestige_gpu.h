@@ -93,6 +93,8 @@ typedef struct pg_info {
   int list_capacity;  /* entries per particle of the pair-pass neighbour lists */
   long long overlap_split;  /* > 0: the continuity pass over slots [0, split) runs beside the
                                neighbour lists of [split, n) (double-word SPH handles) */
+  int block_size;      /* threads per block of the neighbour lists and the continuity pass */
+  int momentum_block;  /* threads per block of the momentum pass */
 } pg_info;
 
 /* Fill *cfg with defaults (3D f64 SPH, gamma 7, alpha 0.1, eps 0.01, multiplier 1). */
@@ -244,12 +246,20 @@ int pg_backward(pg_system* sys, const double* dL_dx, double* dL_dalpha, double* 
 /* Autotuner (SPH handles): time every (cell multiplier 1 or 1/2, arithmetic mode, block size 64,
  * 128 or 256) on the handle's current state for `trial_steps` steps each, keep the fastest whose
  * rates are within the mode's tolerance of the IEEE rates (1e-10 normwise for f64, 1e-4 for
- * f32), apply it and report it.  The handle's state is restored afterwards; a graph-enabled handle
+ * f32), then time the momentum pass's own block size (64, 128, 256) with the rest fixed and the
+ * common block size again with that momentum block, apply the result and report it (the
+ * momentum block in pg_info.momentum_block).  The handle's state is restored afterwards; a graph-enabled handle
  * is re-captured.  No reference counterpart (the reference has no executable backend to tune). */
 int pg_autotune(pg_system* sys, int trial_steps, int* best_block, double* best_multiplier, int* best_f64_mode,
                 double* best_ms_per_step);
-/* Apply a tuning found earlier (e.g. cached by the host) without searching. */
+/* Apply a tuning found earlier (e.g. cached by the host) without searching.  The momentum pass
+ * takes the same block size until pg_set_momentum_block sets its own. */
 int pg_set_tuning(pg_system* sys, int block, double cell_multiplier, int f64_mode);
+/* Block size of the momentum pass alone (64, 128 or 256 threads; 0: the block size of the other
+ * list kernels).  pg_autotune chooses it after the other settings: the momentum pass runs alone
+ * and reads neighbour records that consecutive slots share, so it can prefer larger blocks than
+ * the continuity pass, which shares the SMs with the list kernel. */
+int pg_set_momentum_block(pg_system* sys, int block);
 
 /* Device characterisation: FP64 and FP32 FMA-pipe throughput of the current device in TFLOP/s
  * (two flops per FMA), measured with eight independent FMA chains per thread, 8 blocks of 256

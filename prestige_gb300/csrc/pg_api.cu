@@ -219,6 +219,8 @@ int enqueue_neighbors(pg_system* s) {
   return PG_OK;
 }
 
+int mom_block(const pg_system* s) { return s->block_mom > 0 ? s->block_mom : s->block; }
+
 // Kernels enqueued by one neighbour search (hash, radix passes, cell count, scan).
 long long neighbor_launches(const pg_system* s) { return 1 + 3LL * s->nw.passes + 1 + (s->ncells ? 3 : 0); }
 
@@ -250,7 +252,7 @@ int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
     PG_TRY(launch_sph_list_pass(s->stream, a1, s->arith, SPH_CONT, s->ov_pass_grid, s->block));
     PG_CUDA_TRY(cudaStreamWaitEvent(s->stream, s->ov_ev[1], 0));
     if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
-    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], s->block));
+    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], mom_block(s)));
     s->launches += neighbor_launches(s) + 6;
     if (ev) PG_CUDA_TRY(cudaEventRecord(ev[5], s->stream));
     return PG_OK;
@@ -265,7 +267,7 @@ int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
   } else {
     PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_CONT, s->pass_grid[SPH_CONT], s->block));
     if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
-    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], s->block));
+    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], mom_block(s)));
     s->launches += neighbor_launches(s) + 4;
   }
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[5], s->stream));
@@ -495,7 +497,7 @@ int choose_pass_grid(pg_system* s) {
   PG_CUDA_TRY(cudaGetDevice(&dev));
   PG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   for (int st = 0; st < 3; ++st) {
-    const int occ = sph_list_occupancy(s->arith, s->dim, st, s->block);
+    const int occ = sph_list_occupancy(s->arith, s->dim, st, st == SPH_MOM ? mom_block(s) : s->block);
     s->pass_grid[st] = occ > 0 ? occ * sms : 0;  // persistent: one resident wave
   }
   const int locc = sph_list_occupancy(s->arith, s->dim, -1, s->block);
@@ -649,10 +651,26 @@ int retune_sph(pg_system* s, double mult, int f64_mode, int block) {
   PG_TRY(build_sph_tables(s, gk));
   s->arith = arith_of(s->cfg, s->f64);
   s->block = block;
+  s->block_mom = 0;
   PG_TRY(ensure_sorted_buffers(s));
   PG_TRY(choose_pass_grid(s));
   s->nbr_valid = false;
   return PG_OK;
+}
+
+int set_momentum_block(pg_system* s, int block) {
+  if (s->model != PG_MODEL_SPH) {
+    set_error("tuning applies to SPH handles");
+    return PG_EINVAL;
+  }
+  if (block != 0 && (block < 32 || block > kSphMaxThreads || block % 32)) {
+    set_error("momentum block %d must be 0 or a multiple of 32 in 32..%d", block, kSphMaxThreads);
+    return PG_EINVAL;
+  }
+  PG_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  drop_graphs(s);
+  s->block_mom = block;
+  return choose_pass_grid(s);
 }
 
 // Field lookup: returns the buffer, its element count per particle and whether it is stored
@@ -1357,6 +1375,8 @@ int pg_get_info(pg_system* s, pg_info* info) {
   info->graph = s->graph_enabled ? 1 : 0;
   info->list_capacity = s->list_cap;
   info->overlap_split = (long long)s->ov_split;
+  info->block_size = s->block;
+  info->momentum_block = pg::mom_block(s);
   return PG_OK;
 }
 

@@ -319,6 +319,12 @@ struct DfPairs {
 
   __device__ __forceinline__ Pre fetch(uint32_t t, uint32_t q) const { return fetch_entry(t, q, STAGE == SPH_MOM && fc); }
 
+  // the momentum pass's cache entries are a DRAM stream like the lists (sph_list_pass_kernel)
+  static constexpr bool kL2Entry = STAGE == SPH_MOM;
+  __device__ __forceinline__ void prefetch_entry(uint32_t q) const {
+    if (fc) prefetch_l2(fc + (size_t)q * kListTile);
+  }
+
   // cached: list entry q of a momentum pass that reads F and w from the continuity pass
   __device__ __forceinline__ Pre fetch_entry(uint32_t t, uint32_t q, bool cached) const {
     Pre p;

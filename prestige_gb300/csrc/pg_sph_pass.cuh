@@ -281,6 +281,23 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_kernel(SphArgs a, int
   }
 }
 
+// L2 prefetch hint for one address (PTX prefetch.global.L2; a hint, it returns nothing).
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// List entries (and, for policies with kL2Entry, the policy's own per-entry data through
+// prefetch_entry(q)) are prefetched into L2 this many entries ahead of their use: both are
+// streams from DRAM, read once, that the one-entry-ahead register prefetch cannot cover.
+constexpr uint32_t kL2Ahead = 8;
+
+template <class P, class = void>
+struct L2EntryPolicy {
+  static constexpr bool value = false;
+};
+template <class P>
+struct L2EntryPolicy<P, decltype((void)P::kL2Entry)> {
+  static constexpr bool value = P::kL2Entry;
+};
+
 // Policies that split a pair into fetch(t, q) (the loads for neighbour t, entry q of the list) and
 // pair_with(t, q, fetched).
 template <class P, class = void>
@@ -320,6 +337,10 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_pass_kernel(SphArgs a
       typename Pairs::Pre cur = P.fetch(t, 0);
 #pragma unroll 2
       for (uint32_t q = 0; q < L; ++q) {
+        if (q + kL2Ahead < L) {
+          prefetch_l2(my + (size_t)(q + kL2Ahead) * kListTile);
+          if constexpr (L2EntryPolicy<Pairs>::value) P.prefetch_entry(q + kL2Ahead);
+        }
         const uint32_t tnn = q + 2 < L ? my[(q + 2) * kListTile] : tn;
         const typename Pairs::Pre nxt = P.fetch(tn, q + 1 < L ? q + 1 : q);
         P.pair_with(t, q, cur);

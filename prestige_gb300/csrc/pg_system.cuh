@@ -50,6 +50,7 @@ struct pg_system {
   int pass_grid[3] = {0, 0, 0};  // per SphStage
   int list_grid = 0;
   int block = 128;               // threads per block of the list-based SPH kernels
+  int block_mom = 0;             // threads per block of the momentum pass (0: block)
   int list_cap = 128;            // neighbour-list slots per particle
   // overlap of the continuity pass over slots [0, split) with the list kernel over [split, n) on
   // the auxiliary stream (split 0: off); reduced persistent grids let both kernels share the SMs
@@ -110,6 +111,8 @@ long long neighbor_launches(const pg_system* s);
 int sync_and_check(pg_system* s);
 int choose_pass_grid(pg_system* s);
 int retune_sph(pg_system* s, double mult, int f64_mode, int block);
+int mom_block(const pg_system* s);
+int set_momentum_block(pg_system* s, int block);
 int enqueue_step(pg_system* s);
 int apply_io_inputs(pg_system* s);
 void drop_graphs(pg_system* s);

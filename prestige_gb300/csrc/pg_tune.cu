@@ -9,7 +9,10 @@
 //   arithmetic mode (f64: IEEE double or double-word; f32: IEEE single or contracted): a fast
 //     mode is accepted only if its rates at the current state are within the mode's tolerance
 //     of the IEEE rates (1e-10 normwise for f64, 1e-4 for f32);
-//   block size 64, 128 or 256 threads (the pair passes are persistent: one resident wave).
+//   block size 64, 128 or 256 threads, then the momentum pass's own block size with the rest
+//   fixed (it runs alone and shares neighbour records between consecutive slots, so it can
+//   prefer larger blocks than the kernels that share the SMs), then the common block size again
+//   with the momentum block fixed.
 // The state is restored after every trial and at the end; a graph-enabled handle is re-captured
 // with the chosen settings.
 #include <cuda_runtime.h>
@@ -194,6 +197,18 @@ int pg_set_tuning(pg_system* s, int block, double cell_multiplier, int f64_mode)
   return PG_OK;
 }
 
+int pg_set_momentum_block(pg_system* s, int block) {
+  pg::clear_error();
+  if (!s) {
+    pg::set_error("null handle");
+    return PG_EINVAL;
+  }
+  const bool graph = s->graph_enabled;
+  PG_TRY(pg::set_momentum_block(s, block));
+  if (graph) PG_TRY(pg::capture_graphs(s));
+  return PG_OK;
+}
+
 int pg_autotune(pg_system* s, int trial_steps, int* best_block, double* best_multiplier, int* best_f64_mode,
                 double* best_ms_per_step) {
   pg::clear_error();
@@ -258,9 +273,43 @@ int pg_autotune(pg_system* s, int trial_steps, int* best_block, double* best_mul
       }
     }
   }
+  // the momentum pass's own block size, with the other settings fixed at the winner
+  int bmom = 0;
+  if (st == PG_OK) st = pg::retune_sph(s, bm, bmode, bblock);
+  double best_mom = -1.0;
+  for (int bi = 0; bi < 3 && st == PG_OK; ++bi) {
+    double ms = 0.0;
+    st = pg::set_momentum_block(s, blocks[bi]);
+    if (st == PG_OK) st = pg::restore_state(s, saved);
+    if (st == PG_OK) st = pg::time_steps(s, 1, &ms);  // warm-up
+    if (st == PG_OK) st = pg::restore_state(s, saved);
+    if (st == PG_OK) st = pg::time_steps(s, trial_steps, &ms);
+    if (st == PG_OK && (best_mom < 0.0 || ms < best_mom)) {
+      best_mom = ms;
+      bmom = blocks[bi];
+    }
+  }
+  if (st == PG_OK && best_mom >= 0.0) best = best_mom;
+  // the common block size again, with the momentum pass's block fixed (the first search ran the
+  // momentum pass at the common block size, which biases it towards the momentum pass's choice)
+  for (int bi = 0; bi < 3 && st == PG_OK; ++bi) {
+    if (blocks[bi] == bblock) continue;
+    double ms = 0.0;
+    st = pg::retune_sph(s, bm, bmode, blocks[bi]);
+    if (st == PG_OK) st = pg::set_momentum_block(s, bmom);
+    if (st == PG_OK) st = pg::restore_state(s, saved);
+    if (st == PG_OK) st = pg::time_steps(s, 1, &ms);  // warm-up
+    if (st == PG_OK) st = pg::restore_state(s, saved);
+    if (st == PG_OK) st = pg::time_steps(s, trial_steps, &ms);
+    if (st == PG_OK && ms < best) {
+      best = ms;
+      bblock = blocks[bi];
+    }
+  }
   // apply the winner (or, after a failure, the original settings) and restore the state
-  const int st_apply = pg::retune_sph(s, st == PG_OK ? bm : mult0, st == PG_OK ? bmode : mode0,
-                                      st == PG_OK ? bblock : block0);
+  int st_apply = pg::retune_sph(s, st == PG_OK ? bm : mult0, st == PG_OK ? bmode : mode0,
+                                st == PG_OK ? bblock : block0);
+  if (st == PG_OK && st_apply == PG_OK) st_apply = pg::set_momentum_block(s, bmom);
   const int st_restore = pg::restore_state(s, saved);
   s->timing = timing;
   if (st == PG_OK) st = st_apply;

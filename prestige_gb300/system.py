@@ -277,6 +277,7 @@ class ParticleSystem:
             if key in table:
                 t = table[key]
                 self.set_tuning(t["block_size"], t["cell_multiplier"], t["f64_mode"])
+                self.set_momentum_block(t.get("momentum_block", 0))
                 return dict(t, cached=True)
         blk = ctypes.c_int()
         mult = ctypes.c_double()
@@ -285,7 +286,7 @@ class ParticleSystem:
         nat.check(self._lib.pg_autotune(self._h, int(trial_steps), ctypes.byref(blk), ctypes.byref(mult),
                                         ctypes.byref(mode), ctypes.byref(ms)), "pg_autotune")
         res = {"block_size": blk.value, "cell_multiplier": mult.value, "f64_mode": mode.value,
-               "ms_per_step": ms.value}
+               "momentum_block": self.info()["momentum_block"], "ms_per_step": ms.value}
         if cache is not None:
             table = {}
             if os.path.exists(cache):
@@ -301,6 +302,10 @@ class ParticleSystem:
     def set_tuning(self, block_size, cell_multiplier, f64_mode):
         nat.check(self._lib.pg_set_tuning(self._h, int(block_size), float(cell_multiplier), int(f64_mode)),
                   "pg_set_tuning")
+
+    def set_momentum_block(self, block_size):
+        """Block size of the momentum pass alone (0: the other list kernels' block size)."""
+        nat.check(self._lib.pg_set_momentum_block(self._h, int(block_size)), "pg_set_momentum_block")
 
     def info(self):
         i = nat.PgInfo()

@@ -81,6 +81,9 @@ def test_autotune_cache_round_trip(pg, tmp_path):
     second = s2.autotune(trial_steps=1, cache=cache)
     assert second["cached"] is True
     assert second["block_size"] == first["block_size"]
+    assert first["momentum_block"] in (64, 128, 256)
+    assert s2.info()["momentum_block"] == first["momentum_block"]
+    assert s2.info()["block_size"] == first["block_size"]
     assert s2.info()["pass_grid"] > 0
     s.close()
     s2.close()
@@ -91,4 +94,45 @@ def test_autotune_rejects_dem(pg):
     s = ParticleSystem(w["config"], w["n"])
     with pytest.raises(Exception):
         s.autotune(trial_steps=1)
+    s.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_momentum_block_ieee_is_bit_exact(pg, oracle, graph):
+    """The momentum pass's own block size changes the schedule only: IEEE mode stays bit-exact
+    with the oracle for every momentum block, eager and from a graph."""
+    w = workloads.sph_lattice_3d(n=4000, seed=34)
+    s, cfg = _system(w)
+    s.set_tuning(64, 1.0, 0)
+    if graph:
+        s.enable_graph(True)
+    for mb in (256, 128, 0):
+        s.set_momentum_block(mb)
+        info = s.info()
+        assert info["momentum_block"] == (mb or 64) and info["block_size"] == 64
+        assert info["graph"] == (1 if graph else 0)
+    s.set_momentum_block(256)
+    s.step(2)
+    f = w["fields"]
+    st = oracle.SphState(f["pos"], f["vel"], f["rho"], f["mass"])
+    oracle.sph_run(dict(cfg, cell_multiplier=1.0), st, 2)
+    assert np.array_equal(s.get("pos"), st.pos)
+    assert np.array_equal(s.get("rho"), st.rho)
+    s.set_tuning(128, 1.0, 0)  # a new tuning resets the momentum block to the common one
+    assert s.info()["momentum_block"] == 128
+    s.close()
+
+
+def test_momentum_block_errors(pg):
+    from prestige_gb300 import _native as nat
+    w = workloads.sph_lattice_3d(n=500, seed=35)
+    s, _ = _system(w)
+    for bad in (-32, 16, 48, 2048):
+        with pytest.raises(nat.PgError):
+            s.set_momentum_block(bad)
+    s.close()
+    d = workloads.dem_settling(n=500)
+    s = ParticleSystem(d["config"], d["n"])
+    with pytest.raises(nat.PgError):
+        s.set_momentum_block(128)
     s.close()
