@@ -101,6 +101,7 @@ struct NbrWork {
   uint64_t ncells = 0;
   int passes = 0;
   int tiles = 0;
+  int items = 16;  // keys per thread of the radix kernels (tiles of 256 * items keys)
   DevBuf keys[2], vals[2];  // u32
   DevBuf hist;              // u32 [256 * tiles]
   DevBuf digit_total;       // u32 [256]

@@ -23,10 +23,14 @@ namespace pg {
 namespace {
 
 constexpr int kSortThreads = 256;
+// Keys per thread of the histogram and scatter kernels: 16 (tiles of 4096 keys), or 4 (tiles
+// of 1024) for up to kSmallSortN keys, where 4096-key tiles would leave most of the SMs idle
+// (200,000 keys: 49 tiles on 152 SMs).  The result is the same for either tile size.
 constexpr int kSortItems = 16;
+constexpr int kSortItemsSmall = 4;
+constexpr size_t kSmallSortN = size_t(1) << 20;
 constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys per tile
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kWarpChunk = kSortTile / kSortWarps;    // 512 consecutive keys per warp
 constexpr int kRadix = 256;
 
 constexpr int kScanThreads = 1024;
@@ -117,15 +121,16 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const uint32_t
 // ---------------------------------------------------------------------------------------
 // Radix sort passes.
 // ---------------------------------------------------------------------------------------
+template <int ITEMS>
 __global__ void __launch_bounds__(kSortThreads) digit_hist_kernel(const uint32_t* __restrict__ keys, size_t n,
                                                                   int shift, int tiles,
                                                                   uint32_t* __restrict__ hist) {
   __shared__ uint32_t cnt[kRadix];
   cnt[threadIdx.x] = 0;
   __syncthreads();
-  const size_t base = (size_t)blockIdx.x * kSortTile;
+  const size_t base = (size_t)blockIdx.x * (kSortThreads * ITEMS);
 #pragma unroll 4
-  for (int it = 0; it < kSortItems; ++it) {
+  for (int it = 0; it < ITEMS; ++it) {
     const size_t i = base + (size_t)it * kSortThreads + threadIdx.x;
     if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 0xffu], 1u);
   }
@@ -149,10 +154,11 @@ __global__ void __launch_bounds__(kSortThreads) digit_scan_kernel(uint32_t* __re
   if (threadIdx.x == 0) digit_total[blockIdx.x] = carry;
 }
 
-// Stable scatter of one tile.  Warp w owns keys [base + w*512, base + (w+1)*512) and walks
-// them in 16 rounds of 32; within a round, lanes with equal digits are ranked by lane
+// Stable scatter of one tile of 256 * ITEMS keys.  Warp w owns the w-th run of 32 * ITEMS keys
+// and walks it in ITEMS rounds of 32; within a round, lanes with equal digits are ranked by lane
 // (match mask), and a per-warp running count per digit carries the rank across rounds.
 // Warps are then ordered by an exclusive scan of the per-warp counts per digit.
+template <int ITEMS>
 __global__ void __launch_bounds__(kSortThreads) digit_scatter_kernel(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ keys_out,
     uint32_t* __restrict__ vals_out, size_t n, int shift, int tiles, const uint32_t* __restrict__ hist,
@@ -170,11 +176,11 @@ __global__ void __launch_bounds__(kSortThreads) digit_scatter_kernel(
   for (int w = 0; w < kSortWarps; ++w) wcnt[w][tid] = 0;
   __syncthreads();
 
-  const size_t base = (size_t)blockIdx.x * kSortTile + (size_t)warp * kWarpChunk;
+  const size_t base = (size_t)blockIdx.x * (kSortThreads * ITEMS) + (size_t)warp * (32 * ITEMS);
   const uint32_t lt_mask = (1u << lane) - 1u;
-  uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+  uint32_t key[ITEMS], val[ITEMS], rank[ITEMS];
 #pragma unroll
-  for (int r = 0; r < kSortItems; ++r) {
+  for (int r = 0; r < ITEMS; ++r) {
     const size_t i = base + (size_t)r * 32 + lane;
     const bool valid = i < n;
     key[r] = valid ? keys_in[i] : 0u;
@@ -203,7 +209,7 @@ __global__ void __launch_bounds__(kSortThreads) digit_scatter_kernel(
   }
   __syncthreads();
 #pragma unroll
-  for (int r = 0; r < kSortItems; ++r) {
+  for (int r = 0; r < ITEMS; ++r) {
     const size_t i = base + (size_t)r * 32 + lane;
     if (i < n) {
       const uint32_t d = (key[r] >> shift) & 0xffu;
@@ -251,7 +257,9 @@ int NbrWork::init(size_t n_, uint64_t ncells_) {
   ncells = ncells_;
   const int bits = bits_needed(ncells ? ncells - 1 : 0);
   passes = (bits + 7) / 8;
-  tiles = (int)((n + kSortTile - 1) / kSortTile);
+  items = n <= kSmallSortN ? kSortItemsSmall : kSortItems;
+  const size_t tile = (size_t)kSortThreads * items;
+  tiles = (int)((n + tile - 1) / tile);
   if (tiles < 1) tiles = 1;
   const size_t nn = n ? n : 1;
   PG_TRY(keys[0].ensure(nn * 4));
@@ -276,12 +284,21 @@ int sort_and_table(cudaStream_t st, NbrWork& w) {
   int cur = 0;
   for (int p = 0; p < w.passes; ++p) {
     const int shift = 8 * p;
-    digit_hist_kernel<<<w.tiles, kSortThreads, 0, st>>>(w.keys[cur].as<uint32_t>(), n, shift, w.tiles,
-                                                        w.hist.as<uint32_t>());
+    if (w.items == kSortItemsSmall)
+      digit_hist_kernel<kSortItemsSmall><<<w.tiles, kSortThreads, 0, st>>>(w.keys[cur].as<uint32_t>(), n, shift,
+                                                                          w.tiles, w.hist.as<uint32_t>());
+    else
+      digit_hist_kernel<kSortItems><<<w.tiles, kSortThreads, 0, st>>>(w.keys[cur].as<uint32_t>(), n, shift, w.tiles,
+                                                                     w.hist.as<uint32_t>());
     digit_scan_kernel<<<kRadix, kSortThreads, 0, st>>>(w.hist.as<uint32_t>(), w.tiles, w.digit_total.as<uint32_t>());
-    digit_scatter_kernel<<<w.tiles, kSortThreads, 0, st>>>(
-        w.keys[cur].as<uint32_t>(), w.vals[cur].as<uint32_t>(), w.keys[cur ^ 1].as<uint32_t>(),
-        w.vals[cur ^ 1].as<uint32_t>(), n, shift, w.tiles, w.hist.as<uint32_t>(), w.digit_total.as<uint32_t>());
+    if (w.items == kSortItemsSmall)
+      digit_scatter_kernel<kSortItemsSmall><<<w.tiles, kSortThreads, 0, st>>>(
+          w.keys[cur].as<uint32_t>(), w.vals[cur].as<uint32_t>(), w.keys[cur ^ 1].as<uint32_t>(),
+          w.vals[cur ^ 1].as<uint32_t>(), n, shift, w.tiles, w.hist.as<uint32_t>(), w.digit_total.as<uint32_t>());
+    else
+      digit_scatter_kernel<kSortItems><<<w.tiles, kSortThreads, 0, st>>>(
+          w.keys[cur].as<uint32_t>(), w.vals[cur].as<uint32_t>(), w.keys[cur ^ 1].as<uint32_t>(),
+          w.vals[cur ^ 1].as<uint32_t>(), n, shift, w.tiles, w.hist.as<uint32_t>(), w.digit_total.as<uint32_t>());
     cur ^= 1;
   }
   w.sorted_cell = w.keys[cur].as<uint32_t>();
@@ -448,10 +465,11 @@ extern "C" int pg_cell_list_noalloc(const double* pos, size_t n, int dim, const 
     noalloc_hash_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ng, pos, (uint32_t)n, kbuf[cur], vbuf[cur]);
     for (int p = 0; p < passes; ++p) {
       const int shift = 8 * p;
-      digit_hist_kernel<<<tiles, kSortThreads, 0, st>>>(kbuf[cur], n, shift, tiles, hist);
+      digit_hist_kernel<kSortItems><<<tiles, kSortThreads, 0, st>>>(kbuf[cur], n, shift, tiles, hist);
       digit_scan_kernel<<<kRadix, kSortThreads, 0, st>>>(hist, tiles, digit_total);
-      digit_scatter_kernel<<<tiles, kSortThreads, 0, st>>>(kbuf[cur], vbuf[cur], kbuf[cur ^ 1], vbuf[cur ^ 1], n,
-                                                           shift, tiles, hist, digit_total);
+      digit_scatter_kernel<kSortItems><<<tiles, kSortThreads, 0, st>>>(kbuf[cur], vbuf[cur], kbuf[cur ^ 1],
+                                                                       vbuf[cur ^ 1], n, shift, tiles, hist,
+                                                                       digit_total);
       cur ^= 1;
     }
   }
