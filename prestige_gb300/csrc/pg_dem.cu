@@ -96,6 +96,28 @@ __global__ void dem_gather_kernel(DemArgs a) {
   a.sF[k] = make_float4((float)a.pos[o], (float)a.pos[o + 1], (float)a.pos[o + 2], (float)a.radius[id]);
 }
 
+// The integrator's f64 divisions (a DFMA sequence each on a 1/64-rate pipe), out of line so
+// that the particles that skip them (no contact force, no torque) do not run them predicated.
+struct D3 {
+  double x, y, z;
+};
+
+__device__ __noinline__ D3 force_per_mass(D3 F, double m, bool m_ok) {
+  D3 r;
+  r.x = is_zero(F.x) && m_ok ? F.x : ddiv(F.x, m);
+  r.y = is_zero(F.y) && m_ok ? F.y : ddiv(F.y, m);
+  r.z = is_zero(F.z) && m_ok ? F.z : ddiv(F.z, m);
+  return r;
+}
+
+__device__ __noinline__ D3 spin_update(D3 w, D3 T, double I, double dt) {
+  D3 r;
+  r.x = dadd(w.x, dmul(dt, ddiv(T.x, I)));
+  r.y = dadd(w.y, dmul(dt, ddiv(T.y, I)));
+  r.z = dadd(w.z, dmul(dt, ddiv(T.z, I)));
+  return r;
+}
+
 __global__ void __launch_bounds__(128) dem_pass_kernel(DemArgs a) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long my_contacts = 0;
@@ -265,10 +287,18 @@ __global__ void __launch_bounds__(128) dem_pass_kernel(DemArgs a) {
     const bool free_t = is_zero(T[0]) && is_zero(T[1]) && is_zero(T[2]);
     const double I = free_t ? 0.0 : dmul(dmul(dmul(0.4, mi), ri), ri);
     const bool m_ok = positive_finite(mi);
+    // F / m: the divisions sit behind a branch that the particles without a contact force skip
+    // (a select would run them for every particle: the f64 division is a sequence of DFMAs)
+    double fm[3] = {F[0], F[1], F[2]};
+    if (!(m_ok && is_zero(F[0]) && is_zero(F[1]) && is_zero(F[2]))) {
+      const D3 q = force_per_mass(D3{F[0], F[1], F[2]}, mi, m_ok);
+      fm[0] = q.x;
+      fm[1] = q.y;
+      fm[2] = q.z;
+    }
 #pragma unroll
     for (int cc = 0; cc < 3; ++cc) {
-      const double fm = (is_zero(F[cc]) && m_ok) ? F[cc] : ddiv(F[cc], mi);
-      const double v = dadd(vi[cc], dmul(K.dt, dadd(fm, K.grav[cc])));
+      const double v = dadd(vi[cc], dmul(K.dt, dadd(fm[cc], K.grav[cc])));
       a.vel[o + cc] = v;
       a.pos[o + cc] = dadd(xi[cc], dmul(K.dt, v));
     }
@@ -277,8 +307,10 @@ __global__ void __launch_bounds__(128) dem_pass_kernel(DemArgs a) {
       for (int cc = 0; cc < 3; ++cc)
         a.omega[o + cc] = is_zero(wi[cc]) ? dadd(wi[cc], dmul(K.dt, T[cc])) : wi[cc];
     } else {
-#pragma unroll
-      for (int cc = 0; cc < 3; ++cc) a.omega[o + cc] = dadd(wi[cc], dmul(K.dt, ddiv(T[cc], I)));
+      const D3 w = spin_update(D3{wi[0], wi[1], wi[2]}, D3{T[0], T[1], T[2]}, I, K.dt);
+      a.omega[o] = w.x;
+      a.omega[o + 1] = w.y;
+      a.omega[o + 2] = w.z;
     }
   }
   // contact count: warp sum, one atomic per warp
