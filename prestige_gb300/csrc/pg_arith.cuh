@@ -95,11 +95,21 @@ __host__ __device__ __forceinline__ void df_split(double x, float* hi, float* lo
 // (nearest, ties to even) and the exact remainder, an integer of at most 30 bits times
 // 2^(e-52), is converted with one integer-to-float rounding and scaled by a power of two.
 // Exponents outside [-70, 126], zeros, infinities and NaNs take the hardware conversions.
+// The hardware-conversion path, out of line: rare exponents only, so the common path does not
+// compute it as well (the f64 conversions run at the 1/64 rate on GB300).
+static __device__ __noinline__ float2 df_split_slow(double x) {
+  float2 r;
+  df_split(x, &r.x, &r.y);
+  return r;
+}
+
 __device__ __forceinline__ void df_split_fast(double x, float* hi, float* lo) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const int e = (int)((b >> 52) & 0x7ff) - 1023;
   if (e < -70 || e > 126) {
-    df_split(x, hi, lo);
+    const float2 r = df_split_slow(x);
+    *hi = r.x;
+    *lo = r.y;
     return;
   }
   const unsigned sign = (unsigned)(b >> 63) << 31;

@@ -129,6 +129,11 @@ __device__ __forceinline__ int cell_coord_d(double x, double lo, double inv, int
 // from the f64 t (8u (|x| + |lo|) inv + 8u |t|, twice the first-order error of the FP32 copies
 // and operations).  When [t - E, t + E] lies inside one cell, or entirely below 0 or above n,
 // that decides the clamped floor; otherwise (near a cell boundary, NaN) the f64 formula runs.
+// The f64 formula, out of line: only particles near a cell boundary run it.
+__device__ __noinline__ int cell_coord_d_call(double x, double lo, double inv, int n) {
+  return cell_coord_d(x, lo, inv, n);
+}
+
 __device__ __forceinline__ int cell_coord_fast(double x, double lo, float lof, double inv, float invf, int n) {
   float xf, xl;
   df_split_fast(x, &xf, &xl);
@@ -141,7 +146,7 @@ __device__ __forceinline__ int cell_coord_fast(double x, double lo, float lof, d
     const int ia = (int)a;
     if (ia == (int)b) return ia;
   }
-  return cell_coord_d(x, lo, inv, n);
+  return cell_coord_d_call(x, lo, inv, n);
 }
 
 __device__ __forceinline__ int cell_coord_f(float x, float lo, float inv, int n) {
