@@ -8,7 +8,8 @@
 // the oracle's stable counting sort.
 //
 // Sort: 8-bit digits, least significant first.  Each pass is three launches:
-//   digit_hist   per tile of 4096 keys, a 256-bin histogram          -> hist[d * tiles + t]
+//   digit_hist   per tile of 1024 keys (4096 without allocation), a 256-bin histogram
+//                                                                   -> hist[d * tiles + t]
 //   digit_scan   per digit, exclusive scan over tiles (in place)    -> digit_total[d]
 //   digit_scatter stable per-tile ranking with warp match masks, then scatter
 // Input order is id order, and every pass is stable, so equal cells stay in id order.
@@ -23,12 +24,14 @@ namespace pg {
 namespace {
 
 constexpr int kSortThreads = 256;
-// Keys per thread of the histogram and scatter kernels: 16 (tiles of 4096 keys), or 4 (tiles
-// of 1024) for up to kSmallSortN keys, where 4096-key tiles would leave most of the SMs idle
-// (200,000 keys: 49 tiles on 152 SMs).  The result is the same for either tile size.
+// Keys per thread of the histogram and scatter kernels.  The handles' sorts use 4 (tiles of 1024
+// keys): against 16 (tiles of 4096) the 200,000-sphere DEM step went from 0.144 to 0.122 ms
+// (49 tiles had left most of the 152 SMs idle) and the 4M-particle neighbour search from 0.304
+// to 0.285 ms.  The no-allocation path keeps 16: its fixed scratch holds the histograms of
+// 4096-key tiles.  The sort result does not depend on the tile size.
 constexpr int kSortItems = 16;
 constexpr int kSortItemsSmall = 4;
-constexpr size_t kSmallSortN = size_t(1) << 20;
+constexpr size_t kSmallSortN = ~size_t(0);
 constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys per tile
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kRadix = 256;
