@@ -280,8 +280,8 @@ struct DfPairs {
   SphDF w;
   double four_h2;
   uint32_t kself;
-  float4* fc;  // per list entry {G.hi, G.lo, w.hi, w.lo} with G = m_j F: written by the continuity
-               // pass, read by the momentum pass
+  float4* fc;  // per list entry {G.hi, G.lo, u.hi, u.lo} with G = m_j F and u = w / (r^2 + eps h^2):
+               // written by the continuity pass, read by the momentum pass
   df xi[3], vi[3], rhoi, Pi;
   dfacc acc[3], dr;
   static constexpr bool kCacheF = STAGE == SPH_CONT || STAGE == SPH_MOM;
@@ -338,24 +338,28 @@ struct DfPairs {
     return p;
   }
 
-  // CACHED: F holds G = m_j F and wv holds w, both from the continuity pass (list entries of a
-  // step's momentum pass).
+  // CACHED: F holds G = m_j F and wv holds u = w / (r^2 + eps h^2), both from the continuity pass
+  // (list entries of a step's momentum pass); r2 is then not computed: the continuity pass wrote
+  // a zero entry for a listed pair it skipped (coincident double-word positions).
   template <bool CHECK, bool CACHED = false>
   __device__ __forceinline__ bool geometry(uint32_t t, const Pre& p, df* d, df& r2, df& F, df& wv, df& mj) const {
     const float4 ah = p.ah, al = p.al;
     d[0] = df_sub_close(xi[0], df_make(ah.x, al.x));
     d[1] = df_sub_close(xi[1], df_make(ah.y, al.y));
     d[2] = DIM == 3 ? df_sub_close(xi[2], df_make(ah.z, al.z)) : df_make(0.f, 0.f);
-    r2 = df_sumsq3(d[0], d[1], d[2]);
-    if (CHECK) {
-      const df gap = df_sub(r2, df_make(w.four_h2[0], w.four_h2[1]));
-      if (fabsf(gap.hi) <= w.band) {
-        if (!exact_neighbor_call<DIM>(Xd, kself, t, four_h2)) return false;
-      } else if (!(gap.hi < 0.f)) {
-        return false;
+    r2 = df_make(0.f, 0.f);
+    if (!CACHED) {
+      r2 = df_sumsq3(d[0], d[1], d[2]);
+      if (CHECK) {
+        const df gap = df_sub(r2, df_make(w.four_h2[0], w.four_h2[1]));
+        if (fabsf(gap.hi) <= w.band) {
+          if (!exact_neighbor_call<DIM>(Xd, kself, t, four_h2)) return false;
+        } else if (!(gap.hi < 0.f)) {
+          return false;
+        }
       }
+      if (!(r2.hi > 0.f)) return false;
     }
-    if (!(r2.hi > 0.f)) return false;
     if (CACHED) {
       F = df_make(p.fw.x, p.fw.y);
     } else {
@@ -382,14 +386,18 @@ struct DfPairs {
     return true;
   }
 
-  // G = m_j F (computed here, or from the cache)
-  __device__ __forceinline__ void momentum(const float4& rpj, const df* d, df r2, df G, df wv) {
-    // artificial viscosity where the pair approaches (w < 0), computed for every pair and then
-    // selected: nearly every warp has lanes on both sides
-    // two sums of positive terms, consumed by the product only
-    const df den = df_mul(df_add_raw(r2, df_make(w.eps_h2[0], w.eps_h2[1])), df_add_raw(rhoi, df_make(rpj.x, rpj.y)));
-    const df av = df_div(df_mul(df_make(w.avk[0], w.avk[1]), wv), den);
-    const df pij = wv.hi < 0.f ? av : df_make(0.f, 0.f);
+  // u = w / (r^2 + eps h^2), the velocity factor of the artificial viscosity, with the sign of w
+  __device__ __forceinline__ df visc_u(df r2, df wv) const {
+    return df_div(wv, df_add_raw(r2, df_make(w.eps_h2[0], w.eps_h2[1])));  // a sum of positive terms
+  }
+
+  // G = m_j F and u (computed here, or from the cache)
+  __device__ __forceinline__ void momentum(const float4& rpj, const df* d, df G, df u) {
+    // artificial viscosity where the pair approaches (w < 0, so u < 0), computed for every pair
+    // and then selected: nearly every warp has lanes on both sides
+    const df den = df_add_raw(rhoi, df_make(rpj.x, rpj.y));  // a sum of positive terms
+    const df av = df_div(df_mul(df_make(w.avk[0], w.avk[1]), u), den);
+    const df pij = u.hi < 0.f ? av : df_make(0.f, 0.f);
     const df ncoef = df_neg(df_mul(df_add_raw(df_add_raw(Pi, df_make(rpj.z, rpj.w)), pij), G));
     dfacc_add_prod(acc[0], ncoef, d[0]);
     dfacc_add_prod(acc[1], ncoef, d[1]);
@@ -398,12 +406,19 @@ struct DfPairs {
 
   template <bool CHECK, bool CACHED>
   __device__ __forceinline__ void terms(uint32_t t, uint32_t q, const Pre& p) {
+    constexpr bool kStore = STAGE == SPH_CONT && !CHECK;  // list entries of the continuity pass
     df d[3], r2, F, wv, mj;
-    if (!geometry<CHECK, CACHED>(t, p, d, r2, F, wv, mj)) return;
+    if (!geometry<CHECK, CACHED>(t, p, d, r2, F, wv, mj)) {
+      if (kStore && fc) fc[q * kListTile] = make_float4(0.f, 0.f, 0.f, 0.f);  // contributes nothing
+      return;
+    }
     const df G = CACHED ? F : df_mul(mj, F);
-    if (STAGE == SPH_CONT && !CHECK && fc) fc[q * kListTile] = make_float4(G.hi, G.lo, wv.hi, wv.lo);
+    if (kStore && fc) {
+      const df u = visc_u(r2, wv);
+      fc[q * kListTile] = make_float4(G.hi, G.lo, u.hi, u.lo);
+    }
     if (kCont) dfacc_add_prod(dr, G, wv);
-    if (kMom) momentum(p.rp, d, r2, G, wv);
+    if (kMom) momentum(p.rp, d, G, CACHED ? wv : visc_u(r2, wv));
   }
 
   // entry q of an exact neighbour list
