@@ -47,10 +47,10 @@ MOM_BYTES = {"f64": 112, "f32": 56}
 # particles, f64 double-word mode), scaled by the particle count.  Most of it is the per-entry
 # cache the continuity pass writes for it (16 B per neighbour) and the neighbour lists (4 B per
 # neighbour): the pass reads cached pair terms instead of recomputing them.
-MOM_TRAFFIC_PER_PARTICLE = {"f64-fast": 1772.0}
+MOM_TRAFFIC_PER_PARTICLE = {"f64-fast": 1739.0}
 # The resource that binds the momentum pass in that capture: FMA-pipe cycles active (% of peak,
 # sm__pipe_fma_cycles_active) and issue slots active (smsp__issue_active).
-MOM_PIPES = {"f64-fast": {"fma_pipe_active_pct": 58.6, "issue_active_pct": 74.5}}
+MOM_PIPES = {"f64-fast": {"fma_pipe_active_pct": 50.9, "issue_active_pct": 68.7}}
 
 # Flops of the method (each +, -, *, / and sqrt of the oracle's f64 step one flop), counted by the
 # oracle's flop census on the 110,592-particle lattice of the same construction (seed 2):
@@ -515,7 +515,7 @@ def run_gpu(args, rank, world, local, pgroup):
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "sph_list_pass_kernel (momentum pass)", "peak_source": peak_src,
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one momentum-pass "
-                                           "launch at 1,000,000 particles (1,772 B per particle: the per-entry cache and the lists), scaled by N"
+                                           "launch at 1,000,000 particles (1,739 B per particle: the per-entry cache and the lists), scaled by N"
                          if traffic else None,
                          "bytes_per_particle": bpp,
                          "pipes_ncu": MOM_PIPES.get("%s-%s" % (args.precision, args.mode)),
