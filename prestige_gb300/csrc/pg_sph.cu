@@ -325,7 +325,7 @@ struct DfPairs {
     if (fc) prefetch_l2(fc + (size_t)q * kListTile);
   }
 
-  // cached: list entry q of a momentum pass that reads F and w from the continuity pass
+  // cached: list entry q of a momentum pass that reads G = m_j F and u from the continuity pass
   __device__ __forceinline__ Pre fetch_entry(uint32_t t, uint32_t q, bool cached) const {
     Pre p;
     p.ah = Rec[t].ah;
