@@ -231,3 +231,52 @@ def test_overlapped_schedule_with_list_overflow(pg, oracle):
     oracle.sph_run(cfg, st, 1)
     assert _rel(s.get("pos"), st.pos) <= F64_TOL
     assert _rel(s.get("rho"), st.rho) <= F64_TOL
+
+
+def _df_split(x):
+    hi = np.float32(x)
+    return hi, np.float32(x - np.float64(hi))
+
+
+def test_fast_mode_pair_below_double_word_resolution(pg, oracle):
+    """Two particles whose f64 positions differ but whose shifted double-word positions
+    (x - min + 8 h) are the same: the exact lists keep the pair (f64 r^2 > 0), the double-word
+    passes cannot resolve it and skip it, and the continuity pass writes a zero per-entry cache
+    entry for it, so the momentum pass adds nothing for it rather than the entry a previous step
+    left there.  The step stays within the f64 bound of the oracle, which keeps the pair."""
+    w = workloads.sph_lattice_3d(n=4096, seed=2)
+    s, cfg = _pair(w, 1, 1)
+    s.step(1)  # the per-entry cache now holds this step's entries
+    f = w["fields"]
+    pos = np.array(f["pos"], np.float64)
+    i, j = 100, 101
+    pad = 8.0 * cfg["h"]
+    moved = None
+    for delta in (2e-16, 1e-16, 5e-17, 2e-17, 1e-17):
+        b = pos[i].copy()
+        b[0] += delta
+        if b[0] == pos[i][0]:
+            continue
+        trial = pos.copy()
+        trial[j] = b
+        mins = trial.min(axis=0)
+        xa, xb = (trial[i] - mins) + pad, (trial[j] - mins) + pad
+        if all(_df_split(xa[c]) == _df_split(xb[c]) for c in range(3)):
+            moved = trial
+            break
+    assert moved is not None, "no separation below the double-word resolution found"
+    d = moved[i] - moved[j]
+    assert 0.0 < float(d @ d) < (2.0 * cfg["h"]) ** 2
+    vel = np.asarray(f["vel"], np.float64)
+    rho = np.asarray(f["rho"], np.float64)
+    s.set("pos", moved)
+    s.set("vel", vel)
+    s.set("rho", rho)
+    st = oracle.SphState(moved, vel, rho, np.asarray(f["mass"], np.float64))
+    s.step(1)
+    oracle.sph_run(cfg, st, 1)
+    assert _rel(s.get("pos"), st.pos) <= F64_TOL
+    dv = np.abs(s.get("vel") - st.vel).max()
+    assert dv <= F64_TOL * max(np.abs(st.vel).max(), cfg["dt"] * 1e3)
+    assert _rel(s.get("rho"), st.rho) <= F64_TOL
+    s.close()
