@@ -133,7 +133,8 @@ int pg_get_field(pg_system* sys, const char* name, void* host, size_t count, int
  * pos/vel/rho/mass/acc/drho, PG_F64 for user fields).
  *   pg_set_field_async  copies `host` into a staging buffer on an input copy stream; every later
  *                       call on the handle (a step, a rates or neighbour call, a field read)
- *                       first moves it into the field.  So inputs for step k+1 upload while
+ *                       first moves it into the field (the buffers trade places; a handle with
+ *                       a captured graph copies it in).  So inputs for step k+1 upload while
  *                       step k runs.
  *   pg_get_field_async  snapshots the field at this point of the handle's work (a device copy)
  *                       and copies the snapshot to `host` on an output copy stream; later steps

@@ -16,6 +16,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "pg_arith.cuh"
@@ -732,7 +733,15 @@ int apply_io_inputs(pg_system* s) {
     sl.pending = false;
     if (!b) continue;
     PG_CUDA_TRY(cudaStreamWaitEvent(s->stream, sl.in_ready, 0));
-    if (sl.in_bytes) PG_CUDA_TRY(cudaMemcpyAsync(b->p, sl.stage.p, sl.in_bytes, cudaMemcpyDeviceToDevice, s->stream));
+    if (!s->graph_enabled && sl.in_bytes && sl.in_bytes == b->bytes && sl.stage.bytes == b->bytes) {
+      // the staging buffer becomes the field and the field the next staging buffer: kernels take
+      // the field pointers when they are enqueued, so no copy is needed (a captured graph holds
+      // the old pointers, hence the copy below for graph handles); the work enqueued before this
+      // point still reads the old field, and the next upload into it waits for in_free
+      std::swap(b->p, sl.stage.p);
+    } else if (sl.in_bytes) {
+      PG_CUDA_TRY(cudaMemcpyAsync(b->p, sl.stage.p, sl.in_bytes, cudaMemcpyDeviceToDevice, s->stream));
+    }
     PG_CUDA_TRY(cudaEventRecord(sl.in_free, s->stream));
     s->nbr_valid = false;
   }
