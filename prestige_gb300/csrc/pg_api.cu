@@ -460,6 +460,7 @@ int capture_graphs(pg_system* s) {
 //   backfilling pass and list-stream priority 7.76
 //   continuity over the rest on the list stream                           7.65 (7.70 without)
 //   splits 0.5 / 0.6 / 0.8 of the slots                                   7.92 / 7.72 / 7.69
+//   the same after the per-entry cache held u (7.02 at 0.7): 0.6 / 0.8    7.02 / 7.05
 // A finer pipeline (the slots in 4, 8 or 16 even chunks, each chunk's continuity pass starting
 // when its lists are done) gave 7.80 / 7.84 / 8.02 ms against 7.76 for two chunks on the same
 // box: lists and continuity add up to about 4.4 ms however they are interleaved, so once the SMs
