@@ -11,7 +11,8 @@ Output: one JSON line (rank 0).  `value` = particle-steps/s over the timed steps
 resident in HBM (CUDA events on the library's stream, max over ranks); `e2e` = the same metric
 through the public C ABI with host buffers (pinned) copied in and out every step, pipelined
 with the asynchronous field calls so the copies overlap the neighbouring steps.  `roofline`
-describes the momentum pass (the step's dominant kernel).  Unless --no-extras, four more
+describes the momentum pass, the step's longest kernel launch (the continuity pass, of about
+the same total time, runs as two launches beside the neighbour lists).  Unless --no-extras, four more
 sections on rank 0: `batched` (512 uneven 2D dam breaks in one handle vs looping the plain
 handles), `adjoint` (backward / forward cost of the differentiable 3D workload), `dem`
 (200,000-sphere settling) and `sweep` (the lattice at 256k, 1M and 4M particles in f64 and f32,
@@ -39,7 +40,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# Algorithmic bytes per particle of the momentum pass (the step's dominant kernel): reads
+# Algorithmic bytes per particle of the momentum pass (the step's longest launch): reads
 # pos, vel, rho', m once and writes pos, vel once.  3D f64: 64 + 48 = 112 B; f32: 56 B.
 MOM_BYTES = {"f64": 112, "f32": 56}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per particle of one momentum-pass
