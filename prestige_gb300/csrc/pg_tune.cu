@@ -134,17 +134,20 @@ __global__ void fma_chains_kernel(T* out, int iters, T a, T b) {
 template <class T>
 int time_fma_chains(cudaStream_t st, void* out, int blocks, int threads, int iters, double* tflops) {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  PG_CUDA_TRY(cudaEventCreate(&e0));
-  PG_CUDA_TRY(cudaEventCreate(&e1));
-  fma_chains_kernel<T><<<blocks, threads, 0, st>>>((T*)out, iters / 10, (T)0.999, (T)1e-3);
-  cudaEventRecord(e0, st);
-  fma_chains_kernel<T><<<blocks, threads, 0, st>>>((T*)out, iters, (T)0.999, (T)1e-3);
-  cudaEventRecord(e1, st);
-  cudaError_t err = cudaEventSynchronize(e1);
+  cudaError_t err = cudaEventCreate(&e0);
+  if (err == cudaSuccess) err = cudaEventCreate(&e1);
   float ms = 0.f;
-  if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  if (err == cudaSuccess) {
+    fma_chains_kernel<T><<<blocks, threads, 0, st>>>((T*)out, iters / 10, (T)0.999, (T)1e-3);
+    cudaEventRecord(e0, st);
+    fma_chains_kernel<T><<<blocks, threads, 0, st>>>((T*)out, iters, (T)0.999, (T)1e-3);
+    cudaEventRecord(e1, st);
+    err = cudaGetLastError();
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
   if (err != cudaSuccess) {
     set_error("FMA chains: %s", cudaGetErrorString(err));
     return PG_ECUDA;
