@@ -1,7 +1,8 @@
 """ctypes face of the CPU oracle (oracle/_build/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the CPU-baseline leg of
-bench.py, as the checker or the timed CPU baseline -- never by the product library.
+bench.py, as the reference results the GPU path is compared with or as the timed CPU baseline
+-- never by the product library.
 
 The oracle restates the method on the CPU (prestige_oracle.hpp).  Parity with the reference is
 unpinned: the reference (dineshadepu/prestige) has no executable numeric path, no numeric tests

@@ -320,7 +320,7 @@ int enqueue_dem_step(pg_system* s, cudaEvent_t* ev) {
 
 constexpr int kStepEvents = 6;
 
-// Events for one timed step, from the pool.
+// Events for one timed step, from the handle's event pool (created once, reused every step).
 int timing_events(pg_system* s, cudaEvent_t** out) {
   while (s->ev_pool.size() < kStepEvents) {
     cudaEvent_t e;
