@@ -144,6 +144,9 @@ class ClockSampler:
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+            self.path = None
 
     def stop(self):
         if self.proc is None:
