@@ -203,6 +203,30 @@ def sph_run(cfg, state, nsteps):
                               int(nsteps))
 
 
+_timing = None
+
+
+def load_timing():
+    """The CPU timing build (cpu_timing.cpp: cell-sorted arrays, lists built once per step,
+    contraction allowed): the CPU baseline bench.py times."""
+    global _timing
+    if _timing is None:
+        _timing = ctypes.CDLL(_build.build_timing())
+        _timing.orc_sph_run_timing.restype = ctypes.c_double
+    return _timing
+
+
+def timing_threads(n=0):
+    return load_timing().orc_timing_threads(int(n))
+
+
+def sph_run_timing(cfg, state, nsteps):
+    """Advance the state in place with the CPU timing build; returns the wall time in seconds."""
+    spec = sph_spec(cfg, state.n)
+    return load_timing().orc_sph_run_timing(ctypes.byref(spec), 1 if state.f64 else 0, ctypes.c_longlong(state.n),
+                                            state.ptrs(), int(nsteps))
+
+
 def sph_flop_census(cfg, state):
     """Counted flops of one oracle SPH step on `state` (f64, not modified): a dict with the
     particle, candidate and neighbour-pair counts, the flops of the continuity and momentum pair

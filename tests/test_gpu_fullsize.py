@@ -1,0 +1,102 @@
+"""Parity at the full sizes of the benchmark workloads.
+
+  * The 4,096,000-particle jittered lattice that bench.py times (160^3, seed 2):
+      IEEE f64: three steps bit-exact against the oracle (checked after the first and third);
+      double-word f64: two steps, each from the oracle's state, within 1e-10 normwise per step.
+  * The 2D dam break at dx = 0.02 (5,000 fluid + 1,518 wall particles) for its 2,000 steps:
+      IEEE f64 bit-exact against the oracle, compared every 200 steps so a failure names the
+      step window.
+
+The oracle runs these on all host threads (about 1 s per 4M-particle step on 16 cores).
+"""
+import numpy as np
+import pytest
+
+from prestige_gb300 import ParticleSystem, make_config, workloads
+
+pytestmark = pytest.mark.gpu
+
+F64_TOL = 1e-10
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def _handle(w, f64_mode):
+    cfg = dict(w["config"], precision=1, f64_mode=f64_mode)
+    s = ParticleSystem(make_config(**cfg), w["n"])
+    workloads.load_into(s, w)
+    return s, cfg
+
+
+def _ostate(oracle, w):
+    f = w["fields"]
+    return oracle.SphState(np.asarray(f["pos"], np.float64), np.asarray(f["vel"], np.float64),
+                           np.asarray(f["rho"], np.float64), np.asarray(f["mass"], np.float64))
+
+
+@pytest.fixture(scope="module")
+def lattice_4m():
+    return workloads.sph_lattice_3d(n=4096000, seed=2)
+
+
+def test_lattice_4m_ieee_bit_exact(pg, oracle, lattice_4m):
+    w = lattice_4m
+    s, cfg = _handle(w, 0)
+    assert s.info()["overlap_split"] == 0  # the IEEE mode keeps the sequential schedule
+    st = _ostate(oracle, w)
+    for k in (1, 2):
+        s.step(k)
+        oracle.sph_run(cfg, st, k)
+        assert np.array_equal(s.get("pos"), st.pos)
+        assert np.array_equal(s.get("vel"), st.vel)
+        assert np.array_equal(s.get("rho"), st.rho)
+    s.close()
+
+
+def test_lattice_4m_double_word_per_step(pg, oracle, lattice_4m):
+    """The bench's mode and schedule (overlapped lists and continuity pass, per-entry cache),
+    eager and replayed as a CUDA graph."""
+    w = lattice_4m
+    s, cfg = _handle(w, 1)
+    assert s.info()["overlap_split"] > 0
+    g, _ = _handle(w, 1)
+    g.enable_graph(True)
+    st = _ostate(oracle, w)
+    for _ in range(2):
+        s.step(1)
+        g.step(1)
+        oracle.sph_run(cfg, st, 1)
+        assert _rel(s.get("pos"), st.pos) <= F64_TOL
+        dv = np.abs(s.get("vel") - st.vel).max()
+        assert dv <= F64_TOL * np.abs(st.vel).max()
+        assert _rel(s.get("rho"), st.rho) <= F64_TOL
+        assert np.array_equal(g.get("pos"), s.get("pos")) and np.array_equal(g.get("rho"), s.get("rho"))
+        for k in ("pos", "vel", "rho"):  # both restart from the oracle's state: the bound is per step
+            s.set(k, getattr(st, k))
+            g.set(k, getattr(st, k))
+    s.close()
+    g.close()
+
+
+def test_dam_break_full_size_2000_steps_ieee_bit_exact(pg, oracle):
+    w = workloads.dam_break_2d(dx=0.02)
+    assert w["n_fluid"] == 5000
+    s, cfg = _handle(w, 0)
+    st = _ostate(oracle, w)
+    p0 = s.get("pos")
+    for window in range(10):
+        s.step(200)
+        oracle.sph_run(cfg, st, 200)
+        end = 200 * (window + 1)
+        assert np.array_equal(s.get("pos"), st.pos), "positions differ by step %d" % end
+        assert np.array_equal(s.get("vel"), st.vel), "velocities differ by step %d" % end
+        assert np.array_equal(s.get("rho"), st.rho), "densities differ by step %d" % end
+    p1 = s.get("pos")
+    nf = w["n_fluid"]
+    assert np.array_equal(p0[nf:], p1[nf:])  # walls fixed
+    assert p1[:nf, 0].max() > 1.2  # the front has advanced from x = 0.99 m
+    s.close()
