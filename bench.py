@@ -12,15 +12,17 @@ resident in HBM (CUDA events on the library's stream, max over ranks); `e2e` = t
 through the public C ABI with host buffers (pinned) copied in and out every step, pipelined
 with the asynchronous field calls so the copies overlap the neighbouring steps.  `roofline`
 describes the momentum pass, the step's longest kernel launch (the continuity pass, of about
-the same total time, runs as two launches beside the neighbour lists).  Unless --no-extras, four more
+the same total time, runs as two launches beside the neighbour lists).  Unless --no-extras, five more
 sections on rank 0: `batched` (512 uneven 2D dam breaks in one handle vs looping the plain
 handles), `adjoint` (backward / forward cost of the differentiable 3D workload), `dem`
-(200,000-sphere settling) and `sweep` (the lattice at 256k, 1M and 4M particles in f64 and f32,
-double-word / fast and IEEE arithmetic).
+(200,000 spheres: the settling run over its 5,000 steps, and a contact-dense compressed lattice),
+`drift` (the double-word trajectory against the IEEE one over whole runs) and `sweep` (the
+lattice at 256k, 1M and 4M particles in f64 and f32, double-word / fast and IEEE arithmetic).
 
 `--impl reference` times the CPU path on the host cores instead: the reference has no executable
 particle path (its code generator returns text, prestige/src/codegen/simple_cpu.rs:3-22), so the
-CPU arm is this project's oracle restatement of the method, OpenMP over all host threads.
+CPU arm is this project's restatement of the method in its CPU timing build (cell-sorted arrays,
+neighbour lists built once per step, OpenMP over all host threads).
 
 Multi-GPU (torchrun): every rank runs an independent replica of the workload on its own GPU
 (replicas only: the plain path is one spatial domain; see the design notes); value = all ranks'
@@ -43,9 +45,12 @@ sys.path.insert(0, ROOT)
 # Algorithmic bytes per particle of the momentum pass (the step's longest launch): reads
 # pos, vel, rho', m once and writes pos, vel once.  3D f64: 64 + 48 = 112 B; f32: 56 B.
 MOM_BYTES = {"f64": 112, "f32": 56}
+# Algorithmic bytes per particle-step of the DEM contact pass with its fused integrator: reads
+# pos, vel, omega (72 B), radius and mass (16 B); writes pos, vel, omega (72 B).
+DEM_BYTES = 160
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per particle of one momentum-pass
-# launch, from the ncu capture summarised in profiles/sph_step_df_lattice3d.md (1,000,000
-# particles, f64 double-word mode), scaled by the particle count.  Most of it is the per-entry
+# launch (sph_list_pass_kernel, SPH_MOM) in an ncu capture at 1,000,000 particles (f64
+# double-word mode), scaled by the particle count.  Most of it is the per-entry
 # cache the continuity pass writes for it (16 B per neighbour) and the neighbour lists (4 B per
 # neighbour): the pass reads cached pair terms instead of recomputing them.
 MOM_TRAFFIC_PER_PARTICLE = {"f64-fast": 1739.0}
@@ -84,7 +89,7 @@ def parse():
                    help="fixed block size of the list kernels instead of the autotuner's (with --cell-mult)")
     p.add_argument("--cell-mult", type=float, default=0.5, help="cell multiplier used with --block")
     p.add_argument("--mom-block", type=int, default=0, help="momentum-pass block size used with --block (0: --block)")
-    p.add_argument("--section", default="all", choices=["all", "batched", "adjoint", "dem", "sweep"],
+    p.add_argument("--section", default="all", choices=["all", "batched", "adjoint", "dem", "sweep", "drift"],
                    help="run only one extra section and print its JSON (for profiling)")
     p.add_argument("--adjoint-steps", type=int, default=500)
     p.add_argument("--adjoint-every", type=int, default=50)
@@ -181,18 +186,46 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def cpu_measure(w, steps, threads):
-    """Oracle (CPU restatement of the method) on `w` for `steps` steps; particle-steps/s."""
+def cpu_model():
+    """Host CPU model name (lscpu), for the CPU-baseline record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return None
+
+
+def cpu_measure(w, steps, threads, warmup=1):
+    """CPU timing build of the step (oracle/cpu_timing.cpp: cell-sorted arrays, neighbour lists
+    built once per step, OpenMP over `threads`) on `w`: the faster of cell multipliers 1 and 1/2
+    in a one-step trial, then `steps` timed steps.  Returns (particle-steps/s, seconds, multiplier)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import py_oracle
-    py_oracle.num_threads(threads)
+    py_oracle.timing_threads(threads)
     f = w["fields"]
     f64 = w["config"]["precision"] == 1
     dt = np.float64 if f64 else np.float32
     st = py_oracle.SphState(np.asarray(f["pos"], dt), np.asarray(f["vel"], dt), np.asarray(f["rho"], dt),
                             np.asarray(f["mass"], dt), f64=f64)
-    sec = py_oracle.sph_run(w["config"], st, steps)
-    return w["n"] * steps / sec, sec
+    trial = {}
+    for mult in (1.0, 0.5):
+        cfg = dict(w["config"], cell_multiplier=mult)
+        py_oracle.sph_run_timing(cfg, st, warmup)
+        trial[mult] = py_oracle.sph_run_timing(cfg, st, 1)
+    mult = min(trial, key=trial.get)
+    sec = py_oracle.sph_run_timing(dict(w["config"], cell_multiplier=mult), st, steps)
+    return w["n"] * steps / sec, sec, mult
+
+
+def cpu_record(value, threads, sample):
+    return {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "cpu_model": cpu_model(), "nproc": os.cpu_count(),
+            "build": "oracle/cpu_timing.cpp: g++ -O3 -ffp-contract=fast -funroll-loops -fopenmp (no -march: the "
+                     "recipe builds on x86 and Arm hosts alike)",
+            "sample": sample}
 
 
 def workload(args, n=None):
@@ -214,27 +247,16 @@ def run_reference(args, rank, world, pgroup):
     threads = cpu_threads()
     n = args.cpu_sample_n or args.n
     w = workload(args, n)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import py_oracle
-    py_oracle.num_threads(threads)
-    f = w["fields"]
-    f64 = args.precision == "f64"
-    dt = np.float64 if f64 else np.float32
-    st = py_oracle.SphState(np.asarray(f["pos"], dt), np.asarray(f["vel"], dt), np.asarray(f["rho"], dt),
-                            np.asarray(f["mass"], dt), f64=f64)
-    if args.warmup:
-        py_oracle.sph_run(w["config"], st, args.warmup)
-    sec = py_oracle.sph_run(w["config"], st, args.steps)
-    value = n * args.steps / sec
+    value, sec, mult = cpu_measure(w, args.steps, threads, warmup=max(args.warmup, 1))
+    sample = ("%d particles x %d steps (after %d warm-up steps and a one-step trial of cell multipliers 1 and "
+              "1/2; %g used), OpenMP over %d threads; the reference has no executable CPU particle path, so "
+              "this is the project's C++ restatement of the method" % (n, args.steps, max(args.warmup, 1), mult,
+                                                                       threads))
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
            "data": "synthetic", "config": config_json(args, n),
-           "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                            "sample": "%d particles x %d steps (after %d warm-up steps), OpenMP over %d threads; "
-                                      "the reference has no executable CPU particle path, so this is the "
-                                      "project's C++ restatement of the method" % (n, args.steps, args.warmup,
-                                                                                   threads)},
+           "cpu_baseline": cpu_record(value, threads, sample),
            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -336,26 +358,99 @@ def bench_adjoint(nsteps=500, every=50, n=100000, modes=("native", "fast")):
     return out
 
 
-def bench_dem(steps=30):
-    """3D DEM settling, 200,000 spheres: particle-steps/s of the full step (graph-replayed)."""
-    import torch
-
+def bench_dem(settle_steps=5000, sample_every=250, dense_steps=20, dense_warmup=3):
+    """3D DEM, 200,000 spheres, f64, device-timed with CUDA events on the library's stream.
+    (a) The settling workload (random sequential insertion, free fall) for its 5,000 steps: every
+        `sample_every` steps one step is timed and its particle-particle contacts counted.
+    (b) A contact-dense case of the same size: spheres on a compressed cubic lattice (50 x 50 x
+        80, 2 % overlap, random velocities and spins) inside touching walls, so every contact path
+        (normal, tangential history, Coulomb slip, torques, walls) runs in the timed steps."""
     from prestige_gb300 import ParticleSystem, workloads
     w = workloads.dem_settling(200000)
     s = ParticleSystem(w["config"], w["n"])
     workloads.load_into(s, w)
-    s.enable_graph(True)
-    s.step(3)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    s.step(steps)
-    t = time.perf_counter() - t0
+    samples = []
+    done = 0
+    while done < settle_steps:
+        s.step(sample_every - 1)
+        s.timing_enable(True)
+        s.step_async(1)
+        s.sync()
+        t = s.timing_read()
+        s.timing_enable(False)
+        done += sample_every
+        samples.append({"step": done, "contacts": s.dem_contacts(), "ms": t["region_ms"], "pass_ms": t["pass_ms"]})
+    s.close()
+    settle_ms = statistics.median([x["ms"] for x in samples])
+    settling = {"workload": "200,000 spheres, r in [0.5, 1.0] mm, random sequential insertion in 0.1 x 0.1 x 0.3 m, "
+                            "kn 1e5, e 0.9, mu 0.3, dt 1e-6, f64, %d steps" % settle_steps,
+                "particles": w["n"], "steps": settle_steps, "timed": "one step in every %d" % sample_every,
+                "ms_per_step_median": settle_ms, "value": w["n"] / (settle_ms * 1e-3),
+                "contacts_max": max(x["contacts"] for x in samples),
+                "contacts_per_sample": [x["contacts"] for x in samples],
+                "note": "the spheres fall together (g t^2 / 2 = 0.12 mm in 5 ms), so pair contacts only start "
+                        "where the lowest spheres meet the floor"}
+    d = workloads.dem_compressed_lattice(nside=(50, 50, 80))
+    s = ParticleSystem(d["config"], d["n"])
+    workloads.load_into(s, d)
+    s.step(dense_warmup)
+    s.timing_enable(True)
+    s.step_async(dense_steps)
+    s.sync()
+    t = s.timing_read()
+    s.timing_enable(False)
     contacts = s.dem_contacts()
     s.close()
-    return {"workload": "200,000 spheres, r in [0.5, 1.0] mm, random sequential insertion in 0.1 x 0.1 x 0.3 m, "
-                        "kn 1e5, e 0.9, mu 0.3, dt 1e-6, f64", "particles": w["n"], "steps": steps,
-            "value": w["n"] * steps / t, "unit": "particle-steps/s", "ms_per_step": 1e3 * t / steps,
-            "contacts_last_step": contacts}
+    ms = t["region_ms"] / dense_steps
+    pass_ms = t["pass_ms"] / dense_steps
+    peak, peak_src = _peak_hbm()
+    achieved = DEM_BYTES * d["n"] / (pass_ms * 1e-3) / 1e9
+    dense = {"workload": "200,000 spheres (50 x 50 x 80) on a cubic lattice spaced 2r (1 - 0.02), r = 0.5 mm, "
+                         "velocities N(0, 0.05) m/s, spins N(0, 50) rad/s, touching walls, f64",
+             "particles": d["n"], "steps": dense_steps, "warmup": dense_warmup, "ms_per_step": ms,
+             "value": d["n"] / (ms * 1e-3), "contacts_last_step": contacts,
+             "stages_ms_per_step": {"neighbor_search": t["neighbor_ms"] / dense_steps,
+                                    "sorted_gather": t["gather_ms"] / dense_steps, "contact_pass": pass_ms},
+             "roofline": {"kernel": "dem_pass_kernel", "bound": "hbm", "bytes_per_particle": DEM_BYTES,
+                          "achieved": achieved, "peak": peak, "peak_source": peak_src, "unit": "GB/s",
+                          "frac": achieved / peak,
+                          "binding_resource": "FP64 pipe (contact law and integrator in IEEE double)"}}
+    return {"settling": settling, "dense": dense, "unit": "particle-steps/s",
+            "timing": "CUDA events on the library's stream"}
+
+
+def bench_drift(n=4096000, lattice_steps=100, lattice_every=10, dam_steps=2000, dam_every=100):
+    """Trajectory drift of the double-word f64 mode: its trajectory against the IEEE f64 one (which
+    reproduces the oracle bit for bit), without resetting the state, on the 4M lattice for 100
+    steps and on the 2D dam break at dx = 0.02 for its 2,000 steps.  Deviation of a field =
+    max_i |a_dw - a_ieee| / max_i |a_ieee|, maximum over the checkpoints."""
+    from prestige_gb300 import ParticleSystem, make_config, workloads
+
+    def run(w, nsteps, every):
+        a = ParticleSystem(make_config(**dict(w["config"], precision=1, f64_mode=0)), w["n"])
+        b = ParticleSystem(make_config(**dict(w["config"], precision=1, f64_mode=1)), w["n"])
+        workloads.load_into(a, w)
+        workloads.load_into(b, w)
+        worst = {"pos": 0.0, "vel": 0.0, "rho": 0.0}
+        for _ in range(every, nsteps + 1, every):
+            a.step(every)
+            b.step(every)
+            for k in worst:
+                ref = a.get(k)
+                worst[k] = max(worst[k], float(np.abs(b.get(k) - ref).max() / np.abs(ref).max()))
+        a.close()
+        b.close()
+        return worst
+
+    lat = run(workloads.sph_lattice_3d(n=n, seed=2), lattice_steps, lattice_every)
+    dam = run(workloads.dam_break_2d(dx=0.02), dam_steps, dam_every)
+    return {"bound": max(max(lat.values()), max(dam.values())),
+            "lattice": {"workload": "sph_lattice_3d, %d particles" % n, "steps": lattice_steps, "max_rel": lat},
+            "dam_break": {"workload": "2D dam break, dx = 0.02 (5,000 fluid + 1,518 wall particles)",
+                          "steps": dam_steps, "max_rel": dam},
+            "against": "IEEE f64 mode (bit-exact with the oracle)",
+            "norm": "max_i |a_dw - a_ieee| / max_i |a_ieee| per field, maximum over checkpoints every %d (lattice) "
+                    "and %d (dam break) steps" % (lattice_every, dam_every)}
 
 
 def bench_sweep(steps=100, warmup=3, sizes=(262144, 1000000, 4096000)):
@@ -407,7 +502,8 @@ def run_gpu(args, rank, world, local, pgroup):
             if args.section == "adjoint":
                 res = bench_adjoint(args.adjoint_steps, args.adjoint_every, modes=args.adjoint_modes.split(","))
             else:
-                res = {"batched": bench_batched, "dem": bench_dem, "sweep": bench_sweep}[args.section]()
+                res = {"batched": bench_batched, "dem": bench_dem, "sweep": bench_sweep,
+                       "drift": bench_drift}[args.section]()
             print(json.dumps({"section": args.section, args.section: res}), flush=True)
         return
     w = workload(args)
@@ -499,12 +595,13 @@ def run_gpu(args, rank, world, local, pgroup):
             threads = cpu_threads()
             cn = args.cpu_sample_n or min(n, 1000000)
             cw = workload(args, cn)
-            csteps = 2
-            cval, csec = cpu_measure(cw, csteps, threads)
-            cpu = {"value": cval, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                   "sample": "%d-particle lattice of the same construction x %d steps (%.1f s), OpenMP over %d "
-                             "threads; the reference has no executable CPU path, so this is the project's C++ "
-                             "restatement of the method" % (cn, csteps, csec, threads)}
+            csteps = 3
+            cval, csec, cmult = cpu_measure(cw, csteps, threads)
+            cpu = cpu_record(cval, threads,
+                             "%d-particle lattice of the same construction x %d steps (%.1f s, cell multiplier %g, "
+                             "the faster of 1 and 1/2), OpenMP over %d threads; the reference has no executable "
+                             "CPU path, so this is the project's C++ restatement of the method"
+                             % (cn, csteps, csec, cmult, threads))
         out = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -558,6 +655,7 @@ def run_gpu(args, rank, world, local, pgroup):
             out["adjoint"] = bench_adjoint(args.adjoint_steps, args.adjoint_every,
                                            modes=args.adjoint_modes.split(","))
             out["dem"] = bench_dem()
+            out["drift"] = bench_drift(n)
             out["sweep"] = bench_sweep()
         print(json.dumps(out), flush=True)
 

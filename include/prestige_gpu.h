@@ -183,10 +183,13 @@ int pg_get_pair_lists(pg_system* sys, uint32_t* lengths, uint32_t* entries, size
  *   stream       a cudaStream_t, or NULL for the default stream; the call only enqueues work
  * Scratch: a fixed device array compiled into the library, about 8.3 MB, held on every device
  * that uses it until the process exits.  n is limited to 1,048,576 particles; larger n gives
- * PG_EINVAL.  The first call on a device looks up the array's device address with
- * cudaGetSymbolAddress; make that first call before any stream capture.  Every call shares the
- * array, so calls whose GPU work overlaps (other streams, unordered host threads) race; order
- * them on one stream. */
+ * PG_EINVAL.  Every call made outside stream capture looks up the array's device address in
+ * the current context with cudaGetSymbolAddress (so a cudaDeviceReset or a different context
+ * is followed); a call made while `stream` is capturing reuses the address of the last call
+ * outside capture on that device, so make one call on each device before capturing
+ * (PG_ESTATE otherwise), in the context the capture will use.  Every call shares the array, so
+ * calls whose GPU work overlaps (other streams, unordered host threads) race; order them on
+ * one stream. */
 int pg_cell_list_noalloc(const double* pos, size_t n, int dim, const double domain_lo[3], const double domain_hi[3],
                          double support, double cell_multiplier, uint32_t* sorted_cell, uint32_t* sorted_id,
                          uint32_t* cell_start, size_t cell_start_capacity, size_t* n_cells, void* stream);

@@ -349,9 +349,12 @@ std::mutex g_noalloc_mu;
 void* g_noalloc_addr[kNoAllocMaxDevices] = {};
 
 // Device address of the scratch array on the current device.  The array's name in host code
-// is only a host-side stand-in, so the address is looked up once per device with that device
-// current and kept.
-int noalloc_scratch(unsigned char** out) {
+// is only a host-side stand-in.  A call made outside stream capture looks the address up with
+// the device current (so a cudaDeviceReset, or another context made current, is picked up) and
+// keeps it per device; a call made while `st` is capturing uses the kept address of the last
+// call outside capture on this device, since a lookup may have to load the module, which
+// capture forbids.
+int noalloc_scratch(cudaStream_t st, unsigned char** out) {
   int dev = 0;
   PG_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kNoAllocMaxDevices) {
@@ -359,8 +362,13 @@ int noalloc_scratch(unsigned char** out) {
               kNoAllocMaxDevices);
     return PG_EINVAL;
   }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+    cudaGetLastError();  // the query itself is refused while another stream captures
+    cap = cudaStreamCaptureStatusActive;
+  }
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
@@ -368,6 +376,10 @@ int noalloc_scratch(unsigned char** out) {
       return PG_ECUDA;
     }
     g_noalloc_addr[dev] = p;
+  } else if (!g_noalloc_addr[dev]) {
+    set_error("the first no-allocation cell list call on device %d was made during stream capture; "
+              "make one call on the device before capturing", dev);
+    return PG_ESTATE;
   }
   *out = (unsigned char*)g_noalloc_addr[dev];
   return PG_OK;
@@ -446,7 +458,7 @@ extern "C" int pg_cell_list_noalloc(const double* pos, size_t n, int dim, const 
     return PG_EINVAL;
   }
   unsigned char* scratch = nullptr;
-  PG_TRY(noalloc_scratch(&scratch));
+  PG_TRY(noalloc_scratch((cudaStream_t)stream, &scratch));
   cudaStream_t st = (cudaStream_t)stream;
   if (n) {
     uint32_t* tmp_keys = (uint32_t*)(scratch + kNoAllocKeysOff);

@@ -68,6 +68,38 @@ def test_noalloc_cell_list_matches_handle_path_twice_in_a_row(pg):
             assert np.array_equal(g, r)
 
 
+@pytest.mark.gpu
+def test_noalloc_cell_list_at_its_size_limit(pg):
+    """Exactly the largest accepted size: the scratch's key, value and histogram areas are full."""
+    w = workloads.sph_lattice_3d(n=MAX_PARTICLES, seed=14, cell_multiplier=0.5)
+    got = _noalloc_cell_list(w)
+    ref = _reference_cell_list(w)
+    for g, r in zip(got, ref):
+        assert np.array_equal(g, r)
+
+
+@pytest.mark.gpu
+def test_noalloc_cell_list_of_no_particles(pg):
+    """n = 0 with null position and sort buffers: only the cell table is written, all zeros."""
+    import torch
+
+    lib = _native.load()
+    w = workloads.sph_lattice_3d(n=1000, seed=2)
+    cfg = w["config"]
+    lo = (ctypes.c_double * 3)(*cfg["domain_lo"])
+    hi = (ctypes.c_double * 3)(*cfg["domain_hi"])
+    ncells = ctypes.c_size_t(0)
+    st = lib.pg_cell_list_noalloc(None, 0, 3, lo, hi, 2.0 * cfg["h"], 1.0, None, None, None, 0,
+                                  ctypes.byref(ncells), None)
+    assert st == _native.PG_EINVAL and ncells.value > 0
+    start = torch.full((ncells.value + 1,), -1, dtype=torch.int32, device="cuda")
+    st = lib.pg_cell_list_noalloc(None, 0, 3, lo, hi, 2.0 * cfg["h"], 1.0, None, None, start.data_ptr(),
+                                  start.numel(), ctypes.byref(ncells), None)
+    assert st == _native.PG_OK, lib.pg_last_error()
+    torch.cuda.synchronize()
+    assert (start.cpu().numpy() == 0).all()
+
+
 def test_noalloc_rejects_sizes_beyond_its_limit(pg):
     lib = _native.load()
     lo = (ctypes.c_double * 3)(0.0, 0.0, 0.0)
