@@ -89,6 +89,7 @@ def parse():
                    help="fixed block size of the list kernels instead of the autotuner's (with --cell-mult)")
     p.add_argument("--cell-mult", type=float, default=0.5, help="cell multiplier used with --block")
     p.add_argument("--mom-block", type=int, default=0, help="momentum-pass block size used with --block (0: --block)")
+    p.add_argument("--ppw", type=int, default=32, help="particles per warp of the pair passes used with --block")
     p.add_argument("--section", default="all", choices=["all", "batched", "adjoint", "dem", "sweep", "drift"],
                    help="run only one extra section and print its JSON (for profiling)")
     p.add_argument("--adjoint-steps", type=int, default=500)
@@ -514,8 +515,10 @@ def run_gpu(args, rank, world, local, pgroup):
     if args.block:
         s.set_tuning(args.block, args.cell_mult, 1 if args.mode == "fast" else 0)
         s.set_momentum_block(args.mom_block)
+        s.set_particles_per_warp(args.ppw)
         tuning = {"block_size": args.block, "momentum_block": s.info()["momentum_block"],
-                  "cell_multiplier": args.cell_mult, "fixed": True}
+                  "particles_per_warp": s.info()["particles_per_warp"], "cell_multiplier": args.cell_mult,
+                  "fixed": True}
     elif not args.no_autotune:  # outside the timed region; the state is restored by the tuner
         tuning = s.autotune(trial_steps=3)
     info = s.info()

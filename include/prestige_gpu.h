@@ -95,6 +95,7 @@ typedef struct pg_info {
                                neighbour lists of [split, n) (double-word SPH handles) */
   int block_size;      /* threads per block of the neighbour lists and the continuity pass */
   int momentum_block;  /* threads per block of the momentum pass */
+  int particles_per_warp;  /* target particles per warp of the continuity and momentum passes */
 } pg_info;
 
 /* Fill *cfg with defaults (3D f64 SPH, gamma 7, alpha 0.1, eps 0.01, multiplier 1). */
@@ -160,9 +161,10 @@ int pg_get_neighbor_list(pg_system* sys, uint64_t* offsets, uint32_t* neighbors,
 /* The neighbour lists the SPH pair passes read, as the last step or pg_compute_rates built them
  * (sorted-slot order of that neighbour search, pg_get_neighbors): slot k has lengths[k] entries,
  * sorted slots in walk order, at entries[k * list_capacity ...] (min(lengths[k], list_capacity)
- * of them; the passes walk on for the rest).  In the f64 fast mode they are exactly the
- * particles within 2h under the f64 test, k itself excluded; in the other modes a superset
- * that the passes test again.  entries may be null (lengths only); capacity counts u32 entries
+ * of them; the passes walk on for the rest).  They are exactly the particles within 2h under
+ * the oracle's test in the system's precision (f64 systems: the f64 test, decided in FP32 away
+ * from the boundary; f32 systems: the IEEE FP32 test), k itself and coincident particles
+ * excluded.  entries may be null (lengths only); capacity counts u32 entries
  * and must be at least n * list_capacity (pg_info.list_capacity). */
 int pg_get_pair_lists(pg_system* sys, uint32_t* lengths, uint32_t* entries, size_t capacity);
 
@@ -250,9 +252,10 @@ int pg_backward(pg_system* sys, const double* dL_dx, double* dL_dalpha, double* 
 /* Autotuner (SPH handles): time every (cell multiplier 1 or 1/2, arithmetic mode, block size 64,
  * 128 or 256) on the handle's current state for `trial_steps` steps each, keep the fastest whose
  * rates are within the mode's tolerance of the IEEE rates (1e-10 normwise for f64, 1e-4 for
- * f32), then time the momentum pass's own block size (64, 128, 256) with the rest fixed and the
- * common block size again with that momentum block, apply the result and report it (the
- * momentum block in pg_info.momentum_block).  The handle's state is restored afterwards; a graph-enabled handle
+ * f32), then time the momentum pass's own block size (64, 128, 256) with the rest fixed, the
+ * common block size again with that momentum block, and, in the tolerance-based modes, the
+ * particles per warp of the pair passes (32, 16, 8), apply the result and report it (the
+ * momentum block and particles per warp in pg_info).  The handle's state is restored afterwards; a graph-enabled handle
  * is re-captured.  No reference counterpart (the reference has no executable backend to tune). */
 int pg_autotune(pg_system* sys, int trial_steps, int* best_block, double* best_multiplier, int* best_f64_mode,
                 double* best_ms_per_step);
@@ -264,6 +267,13 @@ int pg_set_tuning(pg_system* sys, int block, double cell_multiplier, int f64_mod
  * and reads neighbour records that consecutive slots share, so it can prefer larger blocks than
  * the continuity pass, which shares the SMs with the list kernel. */
 int pg_set_momentum_block(pg_system* sys, int block);
+/* Target particles per warp of the continuity and momentum passes: 32 (one thread per particle),
+ * 16 or 8 (two or four threads share a particle's neighbour list, each summing every second or
+ * fourth entry, and their sums are combined in a fixed order).  Only the tolerance-based modes
+ * take 16 or 8 (double-word f64, contracted f32: the summation order changes); the IEEE modes
+ * keep 32 so that they stay bit-exact.  pg_autotune searches it after the block sizes.  No
+ * reference counterpart. */
+int pg_set_particles_per_warp(pg_system* sys, int particles_per_warp);
 
 /* Device characterisation: FP64 and FP32 FMA-pipe throughput of the current device in TFLOP/s
  * (two flops per FMA), measured with eight independent FMA chains per thread, 8 blocks of 256

@@ -45,7 +45,7 @@ class PgInfo(ctypes.Structure):
         ("reach", ctypes.c_int), ("pass_grid", ctypes.c_int), ("sort_passes", ctypes.c_int), ("graph", ctypes.c_int),
         ("grid_n", ctypes.c_int * 3), ("grid_lo", _d3), ("cell_size", ctypes.c_double),
         ("list_capacity", ctypes.c_int), ("overlap_split", ctypes.c_longlong),
-        ("block_size", ctypes.c_int), ("momentum_block", ctypes.c_int),
+        ("block_size", ctypes.c_int), ("momentum_block", ctypes.c_int), ("particles_per_warp", ctypes.c_int),
     ]
 
 
@@ -95,6 +95,7 @@ SIGNATURES = {
                          ctypes.POINTER(ctypes.c_double)]),
     "pg_set_tuning": (_I, [_P, _I, ctypes.c_double, _I]),
     "pg_set_momentum_block": (_I, [_P, _I]),
+    "pg_set_particles_per_warp": (_I, [_P, _I]),
     "pg_measure_fma_peaks": (_I, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "pg_timing_enable": (_I, [_P, _I]),
     "pg_timing_read": (_I, [_P, ctypes.POINTER(PgTiming)]),

@@ -248,12 +248,12 @@ int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
     PG_CUDA_TRY(cudaEventRecord(s->ov_ev[0], s->stream));
     PG_CUDA_TRY(cudaStreamWaitEvent(s->aux, s->ov_ev[0], 0));
     PG_TRY(launch_sph_list(s->aux, a2, s->arith, s->ov_list_grid, s->block));
-    PG_TRY(launch_sph_list_pass(s->aux, a2, s->arith, SPH_CONT, 0, s->block));  // one block per tile
+    PG_TRY(launch_sph_list_pass(s->aux, a2, s->arith, SPH_CONT, 0, s->block, s->lanes));  // one block per tile
     PG_CUDA_TRY(cudaEventRecord(s->ov_ev[1], s->aux));
-    PG_TRY(launch_sph_list_pass(s->stream, a1, s->arith, SPH_CONT, s->ov_pass_grid, s->block));
+    PG_TRY(launch_sph_list_pass(s->stream, a1, s->arith, SPH_CONT, s->ov_pass_grid, s->block, s->lanes));
     PG_CUDA_TRY(cudaStreamWaitEvent(s->stream, s->ov_ev[1], 0));
     if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
-    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], mom_block(s)));
+    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], mom_block(s), s->lanes));
     s->launches += neighbor_launches(s) + 6;
     if (ev) PG_CUDA_TRY(cudaEventRecord(ev[5], s->stream));
     return PG_OK;
@@ -266,9 +266,9 @@ int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
     if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
     s->launches += neighbor_launches(s) + 3;
   } else {
-    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_CONT, s->pass_grid[SPH_CONT], s->block));
+    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_CONT, s->pass_grid[SPH_CONT], s->block, s->lanes));
     if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
-    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], mom_block(s)));
+    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], mom_block(s), s->lanes));
     s->launches += neighbor_launches(s) + 4;
   }
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[5], s->stream));
@@ -471,7 +471,7 @@ int capture_graphs(pg_system* s) {
 int choose_overlap(pg_system* s, int sms) {
   s->ov_split = 0;
   if (s->model != PG_MODEL_SPH || s->arith != ARITH_F64_DF || s->n < 1000000) return PG_OK;
-  const int rp = sph_list_regs(s->arith, s->dim, SPH_CONT), rl = sph_list_regs(s->arith, s->dim, -1);
+  const int rp = sph_list_regs(s->arith, s->dim, SPH_CONT, s->lanes), rl = sph_list_regs(s->arith, s->dim, -1);
   if (rp <= 0 || rl <= 0) return PG_OK;
   const int per_block_p = ((rp + 7) / 8) * 8 * s->block, per_block_l = ((rl + 7) / 8) * 8 * s->block;
   const int regs = 65536, threads = 2048;
@@ -499,7 +499,7 @@ int choose_pass_grid(pg_system* s) {
   PG_CUDA_TRY(cudaGetDevice(&dev));
   PG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   for (int st = 0; st < 3; ++st) {
-    const int occ = sph_list_occupancy(s->arith, s->dim, st, st == SPH_MOM ? mom_block(s) : s->block);
+    const int occ = sph_list_occupancy(s->arith, s->dim, st, st == SPH_MOM ? mom_block(s) : s->block, s->lanes);
     s->pass_grid[st] = occ > 0 ? occ * sms : 0;  // persistent: one resident wave
   }
   const int locc = sph_list_occupancy(s->arith, s->dim, -1, s->block);
@@ -654,6 +654,7 @@ int retune_sph(pg_system* s, double mult, int f64_mode, int block) {
   s->arith = arith_of(s->cfg, s->f64);
   s->block = block;
   s->block_mom = 0;
+  s->lanes = 1;
   PG_TRY(ensure_sorted_buffers(s));
   PG_TRY(choose_pass_grid(s));
   s->nbr_valid = false;
@@ -672,6 +673,21 @@ int set_momentum_block(pg_system* s, int block) {
   PG_CUDA_TRY(cudaStreamSynchronize(s->stream));
   drop_graphs(s);
   s->block_mom = block;
+  return choose_pass_grid(s);
+}
+
+int set_pass_lanes(pg_system* s, int lanes) {
+  if (s->model != PG_MODEL_SPH) {
+    set_error("tuning applies to SPH handles");
+    return PG_EINVAL;
+  }
+  if (lanes != 1 && lanes != 2 && lanes != 4) {
+    set_error("lanes per particle %d must be 1, 2 or 4 (32, 16 or 8 particles per warp)", lanes);
+    return PG_EINVAL;
+  }
+  PG_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  drop_graphs(s);
+  s->lanes = lanes;
   return choose_pass_grid(s);
 }
 
@@ -1387,6 +1403,7 @@ int pg_get_info(pg_system* s, pg_info* info) {
   info->overlap_split = (long long)s->ov_split;
   info->block_size = s->block;
   info->momentum_block = pg::mom_block(s);
+  info->particles_per_warp = 32 / pg::sph_pass_lanes(s->arith, pg::SPH_MOM, s->lanes);
   return PG_OK;
 }
 

@@ -269,6 +269,15 @@ __device__ __forceinline__ void dfacc_add_prod(dfacc& a, df x, df y) {
   a.lo = a.lo + (s.lo + pl);
 }
 
+// a + b of two accumulators (TwoSum of the high parts, the low parts added)
+__device__ __forceinline__ dfacc dfacc_add(dfacc a, dfacc b) {
+  const df s = two_sum(a.hi, b.hi);
+  dfacc r;
+  r.hi = s.hi;
+  r.lo = (a.lo + b.lo) + s.lo;
+  return r;
+}
+
 __device__ __forceinline__ double dfacc_to_double(dfacc a) { return __dadd_rn((double)a.hi, (double)a.lo); }
 
 }  // namespace pg

@@ -118,8 +118,18 @@ __device__ __noinline__ D3 spin_update(D3 w, D3 T, double I, double dt) {
   return r;
 }
 
-__global__ void __launch_bounds__(128) dem_pass_kernel(DemArgs a) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+// Contacts a thread collects during its candidate walk before it evaluates them.  The walk
+// only tests (FP32 screen, then the exact f64 test); the contact law runs afterwards for the
+// collected contacts, in the order they were found, so the lanes of a warp evaluate their q-th
+// contacts together.  Evaluated inline, each lane's contact ran alone while the others waited
+// (a few contacts per particle among about 200 candidates, at different iterations per lane).
+constexpr int kDemThreads = 128;
+constexpr int kDemBuf = 16;
+
+__global__ void __launch_bounds__(kDemThreads) dem_pass_kernel(DemArgs a) {
+  __shared__ uint32_t s_buf[kDemBuf][kDemThreads];  // [q][thread]: slot of a partner, or kWallId + face
+  const int tid = threadIdx.x;
+  const uint32_t k = blockIdx.x * blockDim.x + tid;
   unsigned long long my_contacts = 0;
   if (k < a.n) {
     const DemK& K = a.K[0];
@@ -163,6 +173,65 @@ __global__ void __launch_bounds__(128) dem_pass_kernel(DemArgs a) {
       }
     };
 
+    // Evaluate the collected contacts in the order found: the geometry of a particle or wall
+    // contact, then the history lookup, the contact law and the history store, shared by both.
+    int nbuf = 0;
+    auto flush = [&]() {
+      for (int q = 0; q < nbuf; ++q) {
+        const uint32_t code = s_buf[q][tid];
+        Contact ct;
+        uint32_t pid;
+        ct.ri = ri;
+        if (code < kWallId) {
+          const uint32_t t = code;
+          pid = a.sorted_id[t];
+          const double4_32a Aj = a.sA[t], Bj = a.sB[t], Wj = a.sW[t];
+          const double d[3] = {dsub(xi[0], Aj.x), dsub(xi[1], Aj.y), dsub(xi[2], Aj.z)};
+          const double d2 = dadd(dadd(dmul(d[0], d[0]), dmul(d[1], d[1])), dmul(d[2], d[2]));
+          const double rs = dadd(ri, Aj.w);
+          const double dist = __dsqrt_rn(d2);
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) ct.nrm[cc] = ddiv(d[cc], dist);
+          ct.delta = dsub(rs, dist);
+          const double wj[3] = {Wj.x, Wj.y, Wj.z};
+          const double vj[3] = {Bj.x, Bj.y, Bj.z};
+          double ws[3], cr[3];
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) ws[cc] = dadd(dmul(ri, wi[cc]), dmul(Aj.w, wj[cc]));
+          cross3(ws, ct.nrm, cr);
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) ct.vr[cc] = dsub(dsub(vi[cc], vj[cc]), cr[cc]);
+          const double mj = Bj.w;
+          ct.meff = ddiv(dmul(mi, mj), dadd(mi, mj));
+        } else {
+          const int face = (int)(code - kWallId);
+          const int ax = face / 2;
+          const bool hi_face = face & 1;
+          const double dist = hi_face ? dsub(K.wall_hi[ax], xi[ax]) : dsub(xi[ax], K.wall_lo[ax]);
+          pid = code;
+          ct.nrm[0] = ct.nrm[1] = ct.nrm[2] = 0.0;
+          ct.nrm[ax] = hi_face ? -1.0 : 1.0;
+          ct.delta = dsub(ri, dist);
+          double ws[3], cr[3];
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) ws[cc] = dmul(ri, wi[cc]);
+          cross3(ws, ct.nrm, cr);
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) ct.vr[cc] = dsub(vi[cc], cr[cc]);
+          ct.meff = mi;
+        }
+        double xo[3], xn[3];
+        lookup(pid, xo);
+        contact_law(K, ct, xo, F, T, xn);
+        store(pid, xn);
+      }
+      nbuf = 0;
+    };
+    auto collect = [&](uint32_t code) {
+      s_buf[nbuf][tid] = code;
+      if (++nbuf == kDemBuf) flush();  // rare: more contacts than the buffer holds
+    };
+
     // FP32 prefilter: |x_i - x_j| < r_i + r_j in f64  =>  the FP32 r^2 below is < thr_j
     // (position and radius rounding to float and the FP32 arithmetic bounded generously)
     const float4 fi = a.sF[k];
@@ -193,44 +262,21 @@ __global__ void __launch_bounds__(128) dem_pass_kernel(DemArgs a) {
     for (int row = 0; row < nrows; ++row) {
       const uint32_t s0 = nb, e0 = ne;
       if (row + 1 < nrows) row_range(row + 1, nb, ne);
-      {
-        for (uint32_t t = s0; t < e0; ++t) {
-          {
-            const float4 fj = a.sF[t];
-            const float d0 = fi.x - fj.x, d1 = fi.y - fj.y, d2 = fi.z - fj.z;
-            const float rr = fi.w + fj.w + slack;
-            if (!(fmaf(d2, d2, fmaf(d1, d1, d0 * d0)) < rr * rr * 1.0000153f)) continue;
-          }
-          const uint32_t j = a.sorted_id[t];
-          if (j == id) continue;
-          const double4_32a Aj = a.sA[t];
-          const double d[3] = {dsub(xi[0], Aj.x), dsub(xi[1], Aj.y), dsub(xi[2], Aj.z)};
-          const double d2 = dadd(dadd(dmul(d[0], d[0]), dmul(d[1], d[1])), dmul(d[2], d[2]));
-          const double rs = dadd(ri, Aj.w);
-          if (!(d2 < dmul(rs, rs))) continue;
-          const double4_32a Bj = a.sB[t], Wj = a.sW[t];
-          Contact ct;
-          const double dist = __dsqrt_rn(d2);
-#pragma unroll
-          for (int cc = 0; cc < 3; ++cc) ct.nrm[cc] = ddiv(d[cc], dist);
-          ct.delta = dsub(rs, dist);
-          const double wj[3] = {Wj.x, Wj.y, Wj.z};
-          const double vj[3] = {Bj.x, Bj.y, Bj.z};
-          double ws[3], cr[3];
-#pragma unroll
-          for (int cc = 0; cc < 3; ++cc) ws[cc] = dadd(dmul(ri, wi[cc]), dmul(Aj.w, wj[cc]));
-          cross3(ws, ct.nrm, cr);
-#pragma unroll
-          for (int cc = 0; cc < 3; ++cc) ct.vr[cc] = dsub(dsub(vi[cc], vj[cc]), cr[cc]);
-          const double mj = Bj.w;
-          ct.meff = ddiv(dmul(mi, mj), dadd(mi, mj));
-          ct.ri = ri;
-          double xo[3], xn[3];
-          lookup(j, xo);
-          contact_law(K, ct, xo, F, T, xn);
-          store(j, xn);
-          ++my_contacts;
+      for (uint32_t t = s0; t < e0; ++t) {
+        {
+          const float4 fj = a.sF[t];
+          const float d0 = fi.x - fj.x, d1 = fi.y - fj.y, d2 = fi.z - fj.z;
+          const float rr = fi.w + fj.w + slack;
+          if (!(fmaf(d2, d2, fmaf(d1, d1, d0 * d0)) < rr * rr * 1.0000153f)) continue;
         }
+        if (t == k) continue;  // the particle itself (slot k holds id)
+        const double4_32a Aj = a.sA[t];
+        const double d[3] = {dsub(xi[0], Aj.x), dsub(xi[1], Aj.y), dsub(xi[2], Aj.z)};
+        const double d2 = dadd(dadd(dmul(d[0], d[0]), dmul(d[1], d[1])), dmul(d[2], d[2]));
+        const double rs = dadd(ri, Aj.w);
+        if (!(d2 < dmul(rs, rs))) continue;
+        collect(t);
+        ++my_contacts;
       }
     }
     for (int face = 0; face < 6; ++face) {
@@ -247,23 +293,9 @@ __global__ void __launch_bounds__(128) dem_pass_kernel(DemArgs a) {
       }
       const double dist = hi_face ? dsub(K.wall_hi[ax], xi[ax]) : dsub(xi[ax], K.wall_lo[ax]);
       if (!(dist < ri)) continue;
-      Contact ct;
-      ct.nrm[0] = ct.nrm[1] = ct.nrm[2] = 0.0;
-      ct.nrm[ax] = hi_face ? -1.0 : 1.0;
-      ct.delta = dsub(ri, dist);
-      double ws[3], cr[3];
-#pragma unroll
-      for (int cc = 0; cc < 3; ++cc) ws[cc] = dmul(ri, wi[cc]);
-      cross3(ws, ct.nrm, cr);
-#pragma unroll
-      for (int cc = 0; cc < 3; ++cc) ct.vr[cc] = dsub(vi[cc], cr[cc]);
-      ct.meff = mi;
-      ct.ri = ri;
-      double xo[3], xn[3];
-      lookup(kWallId + (uint32_t)face, xo);
-      contact_law(K, ct, xo, F, T, xn);
-      store(kWallId + (uint32_t)face, xn);
+      collect(kWallId + (uint32_t)face);
     }
+    flush();  // the lanes of a warp evaluate their collected contacts together
     // Slots after the last contact must read as empty.  The buffer being written held this
     // particle's history of two steps ago, and every history buffer is empty after its first
     // empty slot (initial state, pg_dem_set_history and this loop keep that), so only the
@@ -330,7 +362,7 @@ int launch_dem_gather(cudaStream_t st, const DemArgs& a) {
 
 int launch_dem_pass(cudaStream_t st, const DemArgs& a) {
   if (a.n == 0) return PG_OK;
-  dem_pass_kernel<<<(a.n + 127) / 128, 128, 0, st>>>(a);
+  dem_pass_kernel<<<(a.n + kDemThreads - 1) / kDemThreads, kDemThreads, 0, st>>>(a);
   PG_CUDA_TRY(cudaGetLastError());
   return PG_OK;
 }

@@ -94,9 +94,14 @@ int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith);
 // Neighbour lists for the list-based passes (stage passes read a.nlist / a.nlen / a.nresume).
 // block: threads per block (multiple of 32, <= kSphMaxThreads).
 int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid, int block);
-int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid, int block);
-int sph_list_regs(int arith, int dim, int stage);  // registers per thread of a list kernel (stage < 0) or pass
-int sph_list_occupancy(int arith, int dim, int stage, int block);  // stage < 0: the list kernel
+// lanes: threads per slot of the continuity and momentum passes (1, 2 or 4: 32, 16 or 8
+// particles per warp); only the tolerance-based modes (double-word f64, contracted f32) take
+// more than one, the others run 1 (sph_pass_lanes gives the count a pass actually uses).
+int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid, int block,
+                         int lanes = 1);
+int sph_pass_lanes(int arith, int stage, int lanes);
+int sph_list_regs(int arith, int dim, int stage, int lanes = 1);  // registers per thread of a list kernel (stage < 0) or pass
+int sph_list_occupancy(int arith, int dim, int stage, int block, int lanes = 1);  // stage < 0: the list kernel
 // The list kernel with an explicit FP32 prefilter-position pack a.s[pf_index] (conservative test).
 int launch_sph_list_pf(cudaStream_t st, const SphArgs& a, int pf_index, int grid, int block);
 

@@ -208,15 +208,22 @@ struct RealPairs {
     return p;
   }
 
-  __device__ __forceinline__ void pair(uint32_t t) { pair_with(t, 0, fetch(t, 0)); }
+  // A candidate of the continued walk of an overflowed list (a superset: EXACT_TEST repeats the
+  // oracle's test).
+  __device__ __forceinline__ void pair(uint32_t t) { terms<EXACT_TEST>(t, fetch(t, 0)); }
 
-  __device__ __forceinline__ void pair_with(uint32_t t, uint32_t, const Pre& p) {
+  // A list entry: the lists hold exactly the oracle's neighbours in every mode (f64 lists are
+  // classified with the f64 test, f32 lists with the IEEE FP32 test), so no test is repeated.
+  __device__ __forceinline__ void pair_with(uint32_t t, uint32_t, const Pre& p) { terms<false>(t, p); }
+
+  template <bool TEST>
+  __device__ __forceinline__ void terms(uint32_t t, const Pre& p) {
     const R4 Aj = p.a;
     const R d0 = Ops::sub(xi[0], Aj.x), d1 = Ops::sub(xi[1], Aj.y);
     const R d2 = DIM == 3 ? Ops::sub(xi[2], Aj.z) : R(0);
     R r2 = Ops::add(Ops::mul(d0, d0), Ops::mul(d1, d1));
     if (DIM == 3) r2 = Ops::add(r2, Ops::mul(d2, d2));
-    if (EXACT_TEST) {
+    if (TEST) {
       if (!(r2 < c.four_h2)) return;
       if (!(r2 > R(0))) return;
     }
@@ -243,6 +250,17 @@ struct RealPairs {
       acc[0] = Ops::sub(acc[0], Ops::mul(coef, d0));
       acc[1] = Ops::sub(acc[1], Ops::mul(coef, d1));
       if (DIM == 3) acc[2] = Ops::sub(acc[2], Ops::mul(coef, d2));
+    }
+  }
+
+  // Sum the partial sums of the LANES lanes of a slot (butterfly; every lane ends with the sum).
+  template <int LANES>
+  __device__ __forceinline__ void reduce_lanes() {
+#pragma unroll
+    for (int off = 1; off < LANES; off <<= 1) {
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc) acc[cc] = Ops::add(acc[cc], __shfl_xor_sync(0xffffffffu, acc[cc], off));
+      dr = Ops::add(dr, __shfl_xor_sync(0xffffffffu, dr, off));
     }
   }
 
@@ -429,6 +447,25 @@ struct DfPairs {
   // any candidate (the walk that continues an overflowed list): everything computed here
   __device__ __forceinline__ void pair(uint32_t t) { terms<true, false>(t, 0, fetch_entry(t, 0, false)); }
 
+  // Combine the partial sums of the LANES lanes of a slot (butterfly; every lane ends with the sum).
+  template <int LANES>
+  __device__ __forceinline__ void reduce_lanes() {
+#pragma unroll
+    for (int off = 1; off < LANES; off <<= 1) {
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc) {
+        dfacc o;
+        o.hi = __shfl_xor_sync(0xffffffffu, acc[cc].hi, off);
+        o.lo = __shfl_xor_sync(0xffffffffu, acc[cc].lo, off);
+        acc[cc] = dfacc_add(acc[cc], o);
+      }
+      dfacc o;
+      o.hi = __shfl_xor_sync(0xffffffffu, dr.hi, off);
+      o.lo = __shfl_xor_sync(0xffffffffu, dr.lo, off);
+      dr = dfacc_add(dr, o);
+    }
+  }
+
   __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id, uint32_t k) {
     const SphC<double>& c = K.d;
     if (STAGE == SPH_RATES) {
@@ -460,8 +497,20 @@ struct DfPairs {
 typedef void (*PassKernel)(SphArgs, int);
 
 // Kernel table for the list-based passes and the list kernel (stage < 0).
+template <int DIM, int STAGE, int LANES>
+PassKernel list_pass_lanes(int arith, int* pf_index) {
+  *pf_index = 0;
+  switch (arith) {
+    case ARITH_F64_DF: return sph_list_pass_kernel<DfPairs<DIM, STAGE>, DIM, false, LANES>;
+    case ARITH_F32_FAST: return sph_list_pass_kernel<RealPairs<OpsFF, DIM, false, STAGE>, DIM, true, LANES>;
+    default: return nullptr;
+  }
+}
+
 template <int DIM, int STAGE>
-PassKernel list_pass_for(int arith, int* pf_index) {
+PassKernel list_pass_for(int arith, int* pf_index, int lanes) {
+  if (lanes == 2) return list_pass_lanes<DIM, STAGE, 2>(arith, pf_index);
+  if (lanes == 4) return list_pass_lanes<DIM, STAGE, 4>(arith, pf_index);
   switch (arith) {
     case ARITH_F64_EXACT:
       *pf_index = 3;
@@ -481,17 +530,17 @@ PassKernel list_pass_for(int arith, int* pf_index) {
 }
 
 template <int DIM>
-PassKernel list_kernel_dim(int arith, int stage, int* pf_index) {
+PassKernel list_kernel_dim(int arith, int stage, int lanes, int* pf_index) {
   switch (stage) {
-    case SPH_RATES: return list_pass_for<DIM, SPH_RATES>(arith, pf_index);
-    case SPH_CONT: return list_pass_for<DIM, SPH_CONT>(arith, pf_index);
-    case SPH_MOM: return list_pass_for<DIM, SPH_MOM>(arith, pf_index);
+    case SPH_RATES: return list_pass_for<DIM, SPH_RATES>(arith, pf_index, 1);
+    case SPH_CONT: return list_pass_for<DIM, SPH_CONT>(arith, pf_index, lanes);
+    case SPH_MOM: return list_pass_for<DIM, SPH_MOM>(arith, pf_index, lanes);
     default: break;
   }
   switch (arith) {  // the list kernel
-    case ARITH_F64_EXACT:
+    case ARITH_F64_EXACT:  // exact lists (FP32 prefilter, the f64 test in the band): the passes skip the test
       *pf_index = 3;
-      return sph_list_kernel<DIM, false, -1>;
+      return sph_list_kernel<DIM, false, 0>;
     case ARITH_F64_DF:  // exact lists: the double-word passes skip the neighbour test
       *pf_index = 0;
       return sph_list_kernel<DIM, false, 5>;
@@ -504,11 +553,14 @@ PassKernel list_kernel_dim(int arith, int stage, int* pf_index) {
   }
 }
 
-PassKernel list_kernel(int arith, int dim, int stage, int* pf_index) {
-  return dim == 2 ? list_kernel_dim<2>(arith, stage, pf_index) : list_kernel_dim<3>(arith, stage, pf_index);
+PassKernel list_kernel(int arith, int dim, int stage, int lanes, int* pf_index) {
+  lanes = sph_pass_lanes(arith, stage, lanes);
+  return dim == 2 ? list_kernel_dim<2>(arith, stage, lanes, pf_index)
+                  : list_kernel_dim<3>(arith, stage, lanes, pf_index);
 }
 
-int launch_table(cudaStream_t st, const SphArgs& a, PassKernel kern, int pf, int grid, int block) {
+// lanes: threads per slot of the kernel (1 for the list kernel); a block covers block / lanes slots.
+int launch_table(cudaStream_t st, const SphArgs& a, PassKernel kern, int pf, int grid, int block, int lanes) {
   if (!kern) {
     set_error("unknown arithmetic mode or stage");
     return PG_EINVAL;
@@ -522,7 +574,8 @@ int launch_table(cudaStream_t st, const SphArgs& a, PassKernel kern, int pf, int
     return PG_EINVAL;
   }
   if (a.k_end == a.k_begin) return PG_OK;
-  const uint32_t ntiles = (a.k_end + block - 1) / block - a.k_begin / block;
+  const uint32_t spb = (uint32_t)(block / lanes);
+  const uint32_t ntiles = (a.k_end + spb - 1) / spb - a.k_begin / spb;
   if (grid <= 0 || (uint32_t)grid > ntiles) grid = (int)ntiles;
   kern<<<grid, block, 0, st>>>(a, pf);
   PG_CUDA_TRY(cudaGetLastError());
@@ -576,34 +629,40 @@ int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith) {
   return PG_OK;
 }
 
+int sph_pass_lanes(int arith, int stage, int lanes) {
+  const bool tolerant = arith == ARITH_F64_DF || arith == ARITH_F32_FAST;
+  return tolerant && (stage == SPH_CONT || stage == SPH_MOM) && (lanes == 2 || lanes == 4) ? lanes : 1;
+}
+
 int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid, int block) {
   int pf = 0;
-  PassKernel kern = list_kernel(arith, a.dim, -1, &pf);
-  return launch_table(st, a, kern, pf, grid, block);
+  PassKernel kern = list_kernel(arith, a.dim, -1, 1, &pf);
+  return launch_table(st, a, kern, pf, grid, block, 1);
 }
 
 int launch_sph_list_pf(cudaStream_t st, const SphArgs& a, int pf_index, int grid, int block) {
   PassKernel kern = a.dim == 2 ? sph_list_kernel<2, false, -1> : sph_list_kernel<3, false, -1>;
-  return launch_table(st, a, kern, pf_index, grid, block);
+  return launch_table(st, a, kern, pf_index, grid, block, 1);
 }
 
-int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid, int block) {
+int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid, int block, int lanes) {
   int pf = 0;
-  PassKernel kern = list_kernel(arith, a.dim, stage, &pf);
-  return launch_table(st, a, kern, pf, grid, block);
+  lanes = sph_pass_lanes(arith, stage, lanes);
+  PassKernel kern = list_kernel(arith, a.dim, stage, lanes, &pf);
+  return launch_table(st, a, kern, pf, grid, block, lanes);
 }
 
-int sph_list_regs(int arith, int dim, int stage) {
+int sph_list_regs(int arith, int dim, int stage, int lanes) {
   int pf = 0;
-  PassKernel kern = list_kernel(arith, dim, stage, &pf);
+  PassKernel kern = list_kernel(arith, dim, stage, lanes, &pf);
   cudaFuncAttributes attr;
   if (!kern || cudaFuncGetAttributes(&attr, kern) != cudaSuccess) return 0;
   return attr.numRegs;
 }
 
-int sph_list_occupancy(int arith, int dim, int stage, int block) {
+int sph_list_occupancy(int arith, int dim, int stage, int block, int lanes) {
   int pf = 0, blocks = 0;
-  PassKernel kern = list_kernel(arith, dim, stage, &pf);
+  PassKernel kern = list_kernel(arith, dim, stage, lanes, &pf);
   if (!kern) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, block, 0) != cudaSuccess) return 0;
   return blocks;

@@ -310,16 +310,23 @@ struct PrefetchPolicy<P, decltype((void)P::kPrefetch)> {
 };
 
 // Pair pass over the lists of sph_list_kernel (any block size up to kSphMaxThreads, a
-// multiple of 32).  Lanes step through their lists together;
-// a list that overflowed is followed by the rest of the walk from its resume point.
-template <class Pairs, int DIM, bool EXACT_PF>
+// multiple of 32).  LANES consecutive threads share one target slot (32 / LANES particles per
+// warp): lane `sub` of a slot takes its list entries sub, sub + LANES, ..., the lanes' partial
+// sums are combined by the policy's reduce_lanes<LANES>() (a fixed butterfly, so the result is
+// deterministic) and lane 0 writes the slot's results.  LANES > 1 changes the summation order,
+// so only the tolerance-based modes (double-word f64, contracted f32) use it.  Lanes step
+// through their lists together; a list that overflowed is followed by the rest of the walk from
+// its resume point (lane 0).
+template <class Pairs, int DIM, bool EXACT_PF, int LANES = 1>
 __global__ void __launch_bounds__(kSphMaxThreads) sph_list_pass_kernel(SphArgs a, int pf_index) {
+  static_assert(LANES == 1 || LANES == 2 || LANES == 4, "1, 2 or 4 lanes per slot");
   const int tid = threadIdx.x;
   const uint32_t cap = a.cap;
-  const uint32_t bs = blockDim.x;
-  const uint32_t tile1 = (a.k_end + bs - 1) / bs;
-  for (uint32_t tile = a.k_begin / bs + blockIdx.x; tile < tile1; tile += gridDim.x) {
-    const uint32_t k0 = tile * bs + tid;
+  const uint32_t spb = blockDim.x / LANES;  // slots per block
+  const uint32_t sub = LANES > 1 ? (uint32_t)tid % LANES : 0u;
+  const uint32_t tile1 = (a.k_end + spb - 1) / spb;
+  for (uint32_t tile = a.k_begin / spb + blockIdx.x; tile < tile1; tile += gridDim.x) {
+    const uint32_t k0 = tile * spb + (uint32_t)tid / LANES;
     const bool live = k0 < a.k_end;
     const uint32_t k = live ? k0 : a.n - 1;
     const uint32_t id = a.sorted_id[k];
@@ -332,26 +339,28 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_pass_kernel(SphArgs a
     if constexpr (PrefetchPolicy<Pairs>::value) {
       // software pipeline: list entries two ahead, the neighbour's pack records one ahead; the
       // unrolled pair bodies (branch-free) interleave
-      uint32_t t = L ? my[0] : k;
-      uint32_t tn = L > 1 ? my[kListTile] : t;
-      typename Pairs::Pre cur = P.fetch(t, 0);
+      constexpr uint32_t S = LANES;
+      const uint32_t q0 = sub;
+      uint32_t t = q0 < L ? my[q0 * kListTile] : k;
+      uint32_t tn = q0 + S < L ? my[(q0 + S) * kListTile] : t;
+      typename Pairs::Pre cur = P.fetch(t, q0 < L ? q0 : 0);
 #pragma unroll 2
-      for (uint32_t q = 0; q < L; ++q) {
-        if (q + kL2Ahead < L) {
-          prefetch_l2(my + (size_t)(q + kL2Ahead) * kListTile);
-          if constexpr (L2EntryPolicy<Pairs>::value) P.prefetch_entry(q + kL2Ahead);
+      for (uint32_t q = q0; q < L; q += S) {
+        if (q + kL2Ahead * S < L) {
+          prefetch_l2(my + (size_t)(q + kL2Ahead * S) * kListTile);
+          if constexpr (L2EntryPolicy<Pairs>::value) P.prefetch_entry(q + kL2Ahead * S);
         }
-        const uint32_t tnn = q + 2 < L ? my[(q + 2) * kListTile] : tn;
-        const typename Pairs::Pre nxt = P.fetch(tn, q + 1 < L ? q + 1 : q);
+        const uint32_t tnn = q + 2 * S < L ? my[(q + 2 * S) * kListTile] : tn;
+        const typename Pairs::Pre nxt = P.fetch(tn, q + S < L ? q + S : q);
         P.pair_with(t, q, cur);
         cur = nxt;
         t = tn;
         tn = tnn;
       }
     } else {
-      for (uint32_t q = 0; q < L; ++q) P.pair(my[q * kListTile]);
+      for (uint32_t q = sub; q < L; q += LANES) P.pair(my[q * kListTile]);
     }
-    if (cnt > cap) {
+    if (cnt > cap && sub == 0) {
       // rare: continue the candidate walk where the list stopped
       const float4* __restrict__ PF = (const float4*)a.s[pf_index];
       const SphK* Kp;
@@ -371,7 +380,8 @@ __global__ void __launch_bounds__(kSphMaxThreads) sph_list_pass_kernel(SphArgs a
           if (prefilter_hit<DIM, EXACT_PF>(pi, PF[t], thr)) P.pair(t);
       }
     }
-    if (live) P.finish(a, K, id, k);
+    if constexpr (LANES > 1) P.template reduce_lanes<LANES>();  // whole warps: the tile loop is uniform
+    if (live && sub == 0) P.finish(a, K, id, k);
   }
 }
 

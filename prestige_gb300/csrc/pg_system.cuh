@@ -51,6 +51,7 @@ struct pg_system {
   int list_grid = 0;
   int block = 128;               // threads per block of the list-based SPH kernels
   int block_mom = 0;             // threads per block of the momentum pass (0: block)
+  int lanes = 1;                 // threads per slot of the continuity and momentum passes (32 / particles per warp)
   int list_cap = 128;            // neighbour-list slots per particle
   // overlap of the continuity pass over slots [0, split) with the list kernel over [split, n) on
   // the auxiliary stream (split 0: off); reduced persistent grids let both kernels share the SMs
@@ -113,6 +114,7 @@ int choose_pass_grid(pg_system* s);
 int retune_sph(pg_system* s, double mult, int f64_mode, int block);
 int mom_block(const pg_system* s);
 int set_momentum_block(pg_system* s, int block);
+int set_pass_lanes(pg_system* s, int lanes);
 int enqueue_step(pg_system* s);
 int apply_io_inputs(pg_system* s);
 void drop_graphs(pg_system* s);

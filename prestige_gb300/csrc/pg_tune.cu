@@ -12,7 +12,10 @@
 //   block size 64, 128 or 256 threads, then the momentum pass's own block size with the rest
 //   fixed (it runs alone and shares neighbour records between consecutive slots, so it can
 //   prefer larger blocks than the kernels that share the SMs), then the common block size again
-//   with the momentum block fixed.
+//   with the momentum block fixed;
+//   particles per warp of the continuity and momentum passes (32, 16 or 8: one, two or four
+//   threads per particle, each taking every second or fourth list entry), in the
+//   tolerance-based modes only, with the rest fixed.
 // The state is restored after every trial and at the end; a graph-enabled handle is re-captured
 // with the chosen settings.
 #include <cuda_runtime.h>
@@ -212,6 +215,22 @@ int pg_set_momentum_block(pg_system* s, int block) {
   return PG_OK;
 }
 
+int pg_set_particles_per_warp(pg_system* s, int particles_per_warp) {
+  pg::clear_error();
+  if (!s) {
+    pg::set_error("null handle");
+    return PG_EINVAL;
+  }
+  if (particles_per_warp != 32 && particles_per_warp != 16 && particles_per_warp != 8) {
+    pg::set_error("particles per warp %d must be 32, 16 or 8", particles_per_warp);
+    return PG_EINVAL;
+  }
+  const bool graph = s->graph_enabled;
+  PG_TRY(pg::set_pass_lanes(s, 32 / particles_per_warp));
+  if (graph) PG_TRY(pg::capture_graphs(s));
+  return PG_OK;
+}
+
 int pg_autotune(pg_system* s, int trial_steps, int* best_block, double* best_multiplier, int* best_f64_mode,
                 double* best_ms_per_step) {
   pg::clear_error();
@@ -309,10 +328,28 @@ int pg_autotune(pg_system* s, int trial_steps, int* best_block, double* best_mul
       bblock = blocks[bi];
     }
   }
+  // particles per warp of the pair passes (tolerance-based modes only), the rest fixed
+  int blanes = 1;
+  if (st == PG_OK) st = pg::retune_sph(s, bm, bmode, bblock);
+  if (st == PG_OK) st = pg::set_momentum_block(s, bmom);
+  const int lanes[2] = {2, 4};
+  for (int li = 0; li < 2 && st == PG_OK && pg::sph_pass_lanes(s->arith, pg::SPH_MOM, 2) > 1; ++li) {
+    double ms = 0.0;
+    st = pg::set_pass_lanes(s, lanes[li]);
+    if (st == PG_OK) st = pg::restore_state(s, saved);
+    if (st == PG_OK) st = pg::time_steps(s, 1, &ms);  // warm-up
+    if (st == PG_OK) st = pg::restore_state(s, saved);
+    if (st == PG_OK) st = pg::time_steps(s, trial_steps, &ms);
+    if (st == PG_OK && ms < best) {
+      best = ms;
+      blanes = lanes[li];
+    }
+  }
   // apply the winner (or, after a failure, the original settings) and restore the state
   int st_apply = pg::retune_sph(s, st == PG_OK ? bm : mult0, st == PG_OK ? bmode : mode0,
                                 st == PG_OK ? bblock : block0);
   if (st == PG_OK && st_apply == PG_OK) st_apply = pg::set_momentum_block(s, bmom);
+  if (st == PG_OK && st_apply == PG_OK) st_apply = pg::set_pass_lanes(s, blanes);
   const int st_restore = pg::restore_state(s, saved);
   s->timing = timing;
   if (st == PG_OK) st = st_apply;

@@ -88,6 +88,7 @@ pub struct pg_info {
     pub overlap_split: c_longlong,
     pub block_size: c_int,
     pub momentum_block: c_int,
+    pub particles_per_warp: c_int,
 }
 
 #[repr(C)]
@@ -160,6 +161,7 @@ extern "C" {
                        -> c_int;
     pub fn pg_set_tuning(sys: *mut pg_system, block: c_int, cell_multiplier: c_double, f64_mode: c_int) -> c_int;
     pub fn pg_set_momentum_block(sys: *mut pg_system, block: c_int) -> c_int;
+    pub fn pg_set_particles_per_warp(sys: *mut pg_system, particles_per_warp: c_int) -> c_int;
     pub fn pg_measure_fma_peaks(fp64_tflops: *mut c_double, fp32_tflops: *mut c_double) -> c_int;
 
     pub fn pg_timing_enable(sys: *mut pg_system, enable: c_int) -> c_int;

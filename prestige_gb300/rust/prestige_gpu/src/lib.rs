@@ -211,6 +211,31 @@ impl System {
         Ok(out)
     }
 
+    /// Stage an upload of a named slice (f64 values) on the input copy stream; it takes effect
+    /// before the next call on the handle.
+    ///
+    /// # Safety
+    /// `values` must stay valid and unchanged until `wait_io` returns; page-locked memory lets the
+    /// copy overlap the steps.
+    pub unsafe fn set_async(&mut self, name: &str, values: *const f64, count: usize) -> Result<()> {
+        let n = cname(name)?;
+        check(ffi::pg_set_field_async(self.raw, n.as_ptr(), values as *const c_void, count, ffi::PG_F64))
+    }
+
+    /// Snapshot a named slice now and download it on the output copy stream.
+    ///
+    /// # Safety
+    /// `out` must stay valid for `count` values until `wait_io` returns.
+    pub unsafe fn get_async(&mut self, name: &str, out: *mut f64, count: usize) -> Result<()> {
+        let n = cname(name)?;
+        check(ffi::pg_get_field_async(self.raw, n.as_ptr(), out as *mut c_void, count, ffi::PG_F64))
+    }
+
+    /// Wait for every staged copy and step of the handle; reports device-side errors.
+    pub fn wait_io(&mut self) -> Result<()> {
+        check(unsafe { ffi::pg_wait_io(self.raw) })
+    }
+
     /// Neighbour search (cell hash, stable sort, cell table): per sorted slot its cell and
     /// particle id, and the cell-start table.
     pub fn neighbors(&mut self) -> Result<(Vec<u32>, Vec<u32>, Vec<u32>)> {
@@ -305,6 +330,11 @@ impl System {
 
     pub fn set_tuning(&mut self, block: i32, cell_multiplier: f64, f64_mode: i32) -> Result<()> {
         check(unsafe { ffi::pg_set_tuning(self.raw, block, cell_multiplier, f64_mode) })
+    }
+
+    /// Particles per warp of the continuity and momentum passes (32, 16 or 8).
+    pub fn set_particles_per_warp(&mut self, ppw: i32) -> Result<()> {
+        check(unsafe { ffi::pg_set_particles_per_warp(self.raw, ppw) })
     }
 
     pub fn info(&mut self) -> Result<ffi::pg_info> {

@@ -278,6 +278,7 @@ class ParticleSystem:
                 t = table[key]
                 self.set_tuning(t["block_size"], t["cell_multiplier"], t["f64_mode"])
                 self.set_momentum_block(t.get("momentum_block", 0))
+                self.set_particles_per_warp(t.get("particles_per_warp", 32))
                 return dict(t, cached=True)
         blk = ctypes.c_int()
         mult = ctypes.c_double()
@@ -286,7 +287,8 @@ class ParticleSystem:
         nat.check(self._lib.pg_autotune(self._h, int(trial_steps), ctypes.byref(blk), ctypes.byref(mult),
                                         ctypes.byref(mode), ctypes.byref(ms)), "pg_autotune")
         res = {"block_size": blk.value, "cell_multiplier": mult.value, "f64_mode": mode.value,
-               "momentum_block": self.info()["momentum_block"], "ms_per_step": ms.value}
+               "momentum_block": self.info()["momentum_block"],
+               "particles_per_warp": self.info()["particles_per_warp"], "ms_per_step": ms.value}
         if cache is not None:
             table = {}
             if os.path.exists(cache):
@@ -302,6 +304,11 @@ class ParticleSystem:
     def set_tuning(self, block_size, cell_multiplier, f64_mode):
         nat.check(self._lib.pg_set_tuning(self._h, int(block_size), float(cell_multiplier), int(f64_mode)),
                   "pg_set_tuning")
+
+    def set_particles_per_warp(self, ppw):
+        """Target particles per warp of the continuity and momentum passes (32, 16 or 8; the IEEE
+        modes always run 32)."""
+        nat.check(self._lib.pg_set_particles_per_warp(self._h, int(ppw)), "pg_set_particles_per_warp")
 
     def set_momentum_block(self, block_size):
         """Block size of the momentum pass alone (0: the other list kernels' block size)."""

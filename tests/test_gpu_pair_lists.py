@@ -1,12 +1,12 @@
 """The neighbour lists the SPH pair passes read (pg_get_pair_lists) vs the oracle's neighbour lists.
 
-In the f64 fast mode the list kernel classifies every candidate exactly: an FP32 test away from
-the support radius, the oracle's f64 test in a narrow band around it, so the double-word passes
-need no neighbour test of their own.  Their lists must equal the oracle's f64 neighbour lists
-(traversal order, i itself and coincident particles left out), entry for entry.  The cubic
-spline's gradient vanishes at r = 2h, so a pair misplaced at the boundary would not show in the
-rates: these tests compare the lists themselves, on lattices built so that many pairs sit at
-r = 2h to the last bit.  In the IEEE modes the lists are a superset that the passes test again.
+In both f64 modes (IEEE and double-word) the list kernel classifies every candidate exactly: an
+FP32 test away from the support radius, the oracle's f64 test in a narrow band around it, so the
+pair passes need no neighbour test of their own.  Their lists must equal the oracle's f64
+neighbour lists (traversal order, i itself and coincident particles left out), entry for entry.
+The cubic spline's gradient vanishes at r = 2h, so a pair misplaced at the boundary would not
+show in the rates: these tests compare the lists themselves, on lattices built so that many
+pairs sit at r = 2h to the last bit.
 """
 import numpy as np
 import pytest
@@ -93,29 +93,15 @@ def _pass_lists(s):
     return out
 
 
+@pytest.mark.parametrize("mode", [1, 0])
 @pytest.mark.parametrize("name,make", CASES)
-def test_fast_mode_lists_are_the_exact_neighbours(pg, oracle, name, make):
+def test_f64_lists_are_the_exact_neighbours(pg, oracle, name, make, mode):
     w = make()
-    s, cfg = _system(w, 1)
+    s, cfg = _system(w, mode)
     got = _pass_lists(s)
     ref = _oracle_lists(oracle, w, cfg)
     bad = [i for i in range(w["n"]) if not np.array_equal(got[i], ref[i])]
     assert not bad, "particle %d: %s vs %s" % (bad[0], got[bad[0]], ref[bad[0]])
-
-
-def _is_subsequence(small, big):
-    it = iter(big.tolist())
-    return all(any(x == y for y in it) for x in small.tolist())
-
-
-@pytest.mark.parametrize("name,make", CASES[:2] + CASES[4:5] + CASES[6:7])
-def test_native_mode_lists_contain_the_neighbours_in_order(pg, oracle, name, make):
-    w = make()
-    s, cfg = _system(w, 0)
-    got = _pass_lists(s)
-    ref = _oracle_lists(oracle, w, cfg)
-    bad = [i for i in range(w["n"]) if not _is_subsequence(ref[i], got[i])]
-    assert not bad
 
 
 def test_boundary_cases_exercise_the_band(pg, oracle):

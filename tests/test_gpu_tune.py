@@ -136,3 +136,109 @@ def test_momentum_block_errors(pg):
     with pytest.raises(nat.PgError):
         s.set_momentum_block(128)
     s.close()
+
+
+PPW_CASES = [
+    ("lattice3d", lambda: workloads.sph_lattice_3d(n=4096, seed=2), 1),
+    ("lattice3d_half", lambda: workloads.sph_lattice_3d(n=3000, seed=9, cell_multiplier=0.5), 1),
+    ("dam2d", lambda: workloads.dam_break_2d(dx=0.05), 1),
+    ("lattice3d_f32", lambda: workloads.sph_lattice_3d(n=4096, seed=2, precision=0), 0),
+]
+
+
+@pytest.mark.parametrize("ppw", [16, 8])
+@pytest.mark.parametrize("name,make,f64", PPW_CASES)
+def test_particles_per_warp_steps_within_tolerance(pg, oracle, ppw, name, make, f64):
+    """Two or four threads per particle in the tolerance-based modes: each step (from the
+    oracle's state) within the mode's bound, eager and graph-replayed (the same bits)."""
+    w = make()
+    s, cfg = _system(w, f64_mode=1)
+    s.set_particles_per_warp(ppw)
+    assert s.info()["particles_per_warp"] == ppw
+    g, _ = _system(w, f64_mode=1)
+    g.set_particles_per_warp(ppw)
+    g.enable_graph(True)
+    tol = F64_TOL if f64 else 1e-4
+    dt = np.float64 if f64 else np.float32
+    f = w["fields"]
+    st = oracle.SphState(np.asarray(f["pos"], dt), np.asarray(f["vel"], dt), np.asarray(f["rho"], dt),
+                         np.asarray(f["mass"], dt), f64=bool(f64))
+    for _ in range(3):
+        s.step(1)
+        g.step(1)
+        oracle.sph_run(cfg, st, 1)
+        assert _rel(s.get("pos"), st.pos) <= tol
+        assert np.abs(s.get("vel") - st.vel).max() <= tol * max(np.abs(st.vel).max(), cfg["dt"] * 1e3)
+        assert _rel(s.get("rho"), st.rho) <= tol
+        assert np.array_equal(g.get("pos"), s.get("pos")) and np.array_equal(g.get("rho"), s.get("rho"))
+        for k in ("pos", "vel", "rho"):
+            s.set(k, getattr(st, k))
+            g.set(k, getattr(st, k))
+    s.close()
+    g.close()
+
+
+def test_particles_per_warp_with_overflowed_lists(pg, oracle):
+    """Lists shorter than the neighbourhoods: the lanes share the listed entries and lane 0
+    walks on from the resume point."""
+    w = workloads.sph_lattice_3d(n=3000, seed=21)
+    s, cfg = _system(w, f64_mode=1, list_capacity=16)
+    s.set_particles_per_warp(8)
+    f = w["fields"]
+    st = oracle.SphState(f["pos"], f["vel"], f["rho"], f["mass"])
+    s.step(1)
+    oracle.sph_run(cfg, st, 1)
+    assert _rel(s.get("pos"), st.pos) <= F64_TOL
+    assert _rel(s.get("rho"), st.rho) <= F64_TOL
+    s.close()
+
+
+def test_particles_per_warp_overlapped_schedule(pg, oracle):
+    """1M particles: the overlapped continuity pass and the momentum pass with 16 particles per warp."""
+    w = workloads.sph_lattice_3d(n=1000000, seed=13)
+    s, cfg = _system(w, f64_mode=1)
+    s.set_particles_per_warp(16)
+    assert s.info()["overlap_split"] > 0
+    f = w["fields"]
+    st = oracle.SphState(f["pos"], f["vel"], f["rho"], f["mass"])
+    s.step(1)
+    oracle.sph_run(cfg, st, 1)
+    assert _rel(s.get("pos"), st.pos) <= F64_TOL
+    assert _rel(s.get("rho"), st.rho) <= F64_TOL
+    s.close()
+
+
+def test_particles_per_warp_ieee_stays_bit_exact(pg, oracle):
+    """The IEEE mode keeps one thread per particle whatever is asked, so it stays bit-exact."""
+    w = workloads.sph_lattice_3d(n=4000, seed=33)
+    s, cfg = _system(w, f64_mode=0)
+    s.set_particles_per_warp(8)
+    assert s.info()["particles_per_warp"] == 32
+    f = w["fields"]
+    st = oracle.SphState(f["pos"], f["vel"], f["rho"], f["mass"])
+    s.step(2)
+    oracle.sph_run(cfg, st, 2)
+    assert np.array_equal(s.get("pos"), st.pos) and np.array_equal(s.get("rho"), st.rho)
+    import prestige_gb300._native as nat
+    with pytest.raises(nat.PgError):
+        s.set_particles_per_warp(4)
+    s.close()
+
+
+def test_batched_particles_per_warp(pg, oracle):
+    systems = workloads.batched_dam_breaks(n_systems=5, nmin=400, nmax=1500, seed=8, f64_mode=1)
+    cfgs = [w["config"] for w in systems]
+    b = ParticleSystem.batch(cfgs, [w["n"] for w in systems])
+    for k in ("pos", "vel", "rho", "mass"):
+        b.set(k, np.concatenate([w["fields"][k] for w in systems]))
+    b.set_particles_per_warp(8)
+    b.step(1)
+    pos = b.get("pos")
+    off = 0
+    for w in systems:
+        f = w["fields"]
+        st = oracle.SphState(f["pos"], f["vel"], f["rho"], f["mass"])
+        oracle.sph_run(w["config"], st, 1)
+        assert _rel(pos[off:off + w["n"]], st.pos) <= F64_TOL
+        off += w["n"]
+    b.close()
