@@ -271,6 +271,25 @@ struct AdjPairs {
 //   s5 {abar, 0}   s6 float dbar
 // Per-particle sums (adjoint increments and parameter terms) use Kahan compensation.
 // ---------------------------------------------------------------------------------------
+// Sign of w = v_ij . x_ij from the double-word (hi, lo) records, evaluated in double: true if
+// the pair approaches.  Out of line: only pairs whose FP32 w is within rounding of zero call it.
+// (The records are loaded again here, one component at a time, rather than passed, which keeps
+// the caller's registers.)
+template <int DIM>
+__device__ __noinline__ bool approaches_f64(const float4* XH, const float4* XL, const float4* VH, const float4* VL,
+                                            uint32_t k, uint32_t t) {
+  const float *xh = (const float*)XH, *xl = (const float*)XL, *vh = (const float*)VH, *vl = (const float*)VL;
+  double w = 0.0;
+#pragma unroll 1
+  for (int c = 0; c < DIM; ++c) {
+    const size_t i = 4 * (size_t)k + c, j = 4 * (size_t)t + c;
+    const double d = ((double)xh[i] - (double)xh[j]) + ((double)xl[i] - (double)xl[j]);
+    const double dv = ((double)vh[i] - (double)vh[j]) + ((double)vl[i] - (double)vl[j]);
+    w = fma(dv, d, w);
+  }
+  return w < 0.0;
+}
+
 template <int DIM>
 __global__ void adjoint_prep_f_kernel(SphArgs a) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -318,8 +337,10 @@ struct AdjPairsF {
   float xh[3], xl[3], vh[3], vl[3], ai[3], rhoi, mi, Pi, Pdi, PBi, dbi;
   float gx[3], gv[3], gr, gal, gB;
   float cx[3], cv[3], cr, ca, cb;  // compensation terms (Kahan summation)
+  uint32_t kself;
 
   __device__ __forceinline__ void begin(const SphArgs& a, const SphK& K, uint32_t k) {
+    kself = k;
     XH = (const float4*)a.s[0];
     XL = (const float4*)a.s[1];
     VH = (const float4*)a.s[2];
@@ -433,7 +454,17 @@ struct AdjPairsF {
     const float rb = rhoi + vj.w;
     const float e = r2 + eps_h2;
     float c1 = 0.f, c1a = 0.f;
-    if (w < 0.f) {
+    // The viscosity acts where the pair approaches (w < 0).  The forward pass decided that on
+    // its double-word w; the FP32 w here can carry the wrong sign when |w| is within its rounding
+    // of zero (about 4e-7 of sum |dv_c d_c|), and the derivative of the viscosity jumps there, so
+    // those rare pairs decide in double (approaches_f64, out of line).
+    bool approach = w < 0.f;
+    {
+      float wabs = fabsf(dv[0] * d[0]) + fabsf(dv[1] * d[1]);
+      if (DIM == 3) wabs += fabsf(dv[2] * d[2]);
+      if (fabsf(w) <= 1e-5f * wabs) approach = approaches_f64<DIM>(XH, XL, VH, VL, kself, t);
+    }
+    if (approach) {
       const float base = 1.f / (e * rb);
       c1 = avk * base;
       c1a = avk_alpha * base;

@@ -103,8 +103,10 @@ def test_adjoint_matches_finite_differences(pg, mode):
         vm[i, c] -= ev
         fd = (_forward_loss(w, nsteps, vel=vp) - _forward_loss(w, nsteps, vel=vm)) / (2 * ev)
         # components far below the largest are compared against a floor of the norm: 1e-3 of
-        # the largest for the FP64 adjoint, 1e-1 for the mixed-precision one (FP32 pair terms)
-        scale = max(abs(fd), (1e-3 if mode == 0 else 1e-1) * flat.max())
+        # the largest for the FP64 adjoint, 1e-2 for the mixed-precision one (FP32 pair terms:
+        # measured within 4e-6 of the FP64 adjoint on components above 1e-2 of the largest,
+        # within 3e-5 above 1e-3)
+        scale = max(abs(fd), (1e-3 if mode == 0 else 1e-2) * flat.max())
         assert abs(dv0[i, c] - fd) <= FD_TOL * scale, (i, c, dv0[i, c], fd)
 
 
