@@ -90,7 +90,8 @@ def parse():
     p.add_argument("--cell-mult", type=float, default=0.5, help="cell multiplier used with --block")
     p.add_argument("--mom-block", type=int, default=0, help="momentum-pass block size used with --block (0: --block)")
     p.add_argument("--ppw", type=int, default=32, help="particles per warp of the pair passes used with --block")
-    p.add_argument("--section", default="all", choices=["all", "batched", "adjoint", "dem", "sweep", "drift"],
+    p.add_argument("--section", default="all",
+                   choices=["all", "batched", "adjoint", "dem", "dem_dense", "sweep", "drift"],
                    help="run only one extra section and print its JSON (for profiling)")
     p.add_argument("--adjoint-steps", type=int, default=500)
     p.add_argument("--adjoint-every", type=int, default=50)
@@ -284,6 +285,18 @@ def bench_batched(steps=20, looped_steps=5, sync_steps=2):
     b = ParticleSystem.batch(cfgs, [w["n"] for w in systems])
     for k in ("pos", "vel", "rho", "mass"):
         b.set(k, np.concatenate([w["fields"][k] for w in systems]))
+    # per-stage split of one batched step (eager steps with CUDA events at the stage boundaries)
+    b.step(2)
+    b.timing_enable(True)
+    b.step_async(5)
+    b.sync()
+    tt = b.timing_read()
+    b.timing_enable(False)
+    stages = {"neighbor_search": tt["neighbor_ms"] / 5, "sorted_gather": tt["gather_ms"] / 5,
+              "neighbor_lists": tt["list_ms"] / 5, "continuity_pass": tt["cont_ms"] / 5,
+              "momentum_pass": (tt["pass_ms"] - tt["list_ms"] - tt["cont_ms"]) / 5,
+              "step_eager": tt["region_ms"] / 5}
+    info = b.info()
     b.enable_graph(True)
     b.step(3)
     torch.cuda.synchronize()
@@ -325,7 +338,12 @@ def bench_batched(steps=20, looped_steps=5, sync_steps=2):
             "looped_value": vs, "looped_ms_per_step": 1e3 * ts / sync_steps, "batched_over_looped": vb / vs,
             "looped_async_value": vl, "looped_async_ms_per_step": 1e3 * tl / looped_steps,
             "batched_over_looped_async": vb / vl,
-            "timing": "host wall clock around graph-replayed steps, stream synchronised"}
+            "stages_ms_per_step": stages,
+            "stages_note": ("overlapped: neighbor_lists = lists of the first %d slots; continuity_pass = the "
+                            "continuity pass over them beside the lists of the rest" % info["overlap_split"])
+            if info.get("overlap_split") else "sequential stages",
+            "timing": "host wall clock around graph-replayed steps, stream synchronised; stages from eager "
+                      "steps with CUDA events"}
 
 
 def bench_adjoint(nsteps=500, every=50, n=100000, modes=("native", "fast")):
@@ -366,6 +384,12 @@ def bench_dem(settle_steps=5000, sample_every=250, dense_steps=20, dense_warmup=
     (b) A contact-dense case of the same size: spheres on a compressed cubic lattice (50 x 50 x
         80, 2 % overlap, random velocities and spins) inside touching walls, so every contact path
         (normal, tangential history, Coulomb slip, torques, walls) runs in the timed steps."""
+    return {"settling": bench_dem_settling(settle_steps, sample_every),
+            "dense": bench_dem_dense(dense_steps, dense_warmup), "unit": "particle-steps/s",
+            "timing": "CUDA events on the library's stream"}
+
+
+def bench_dem_settling(settle_steps=5000, sample_every=250):
     from prestige_gb300 import ParticleSystem, workloads
     w = workloads.dem_settling(200000)
     s = ParticleSystem(w["config"], w["n"])
@@ -391,6 +415,11 @@ def bench_dem(settle_steps=5000, sample_every=250, dense_steps=20, dense_warmup=
                 "contacts_per_sample": [x["contacts"] for x in samples],
                 "note": "the spheres fall together (g t^2 / 2 = 0.12 mm in 5 ms), so pair contacts only start "
                         "where the lowest spheres meet the floor"}
+    return settling
+
+
+def bench_dem_dense(dense_steps=20, dense_warmup=3):
+    from prestige_gb300 import ParticleSystem, workloads
     d = workloads.dem_compressed_lattice(nside=(50, 50, 80))
     s = ParticleSystem(d["config"], d["n"])
     workloads.load_into(s, d)
@@ -416,8 +445,7 @@ def bench_dem(settle_steps=5000, sample_every=250, dense_steps=20, dense_warmup=
                           "achieved": achieved, "peak": peak, "peak_source": peak_src, "unit": "GB/s",
                           "frac": achieved / peak,
                           "binding_resource": "FP64 pipe (contact law and integrator in IEEE double)"}}
-    return {"settling": settling, "dense": dense, "unit": "particle-steps/s",
-            "timing": "CUDA events on the library's stream"}
+    return dense
 
 
 def bench_drift(n=4096000, lattice_steps=100, lattice_every=10, dam_steps=2000, dam_every=100):
@@ -503,8 +531,8 @@ def run_gpu(args, rank, world, local, pgroup):
             if args.section == "adjoint":
                 res = bench_adjoint(args.adjoint_steps, args.adjoint_every, modes=args.adjoint_modes.split(","))
             else:
-                res = {"batched": bench_batched, "dem": bench_dem, "sweep": bench_sweep,
-                       "drift": bench_drift}[args.section]()
+                res = {"batched": bench_batched, "dem": bench_dem, "dem_dense": bench_dem_dense,
+                       "sweep": bench_sweep, "drift": bench_drift}[args.section]()
             print(json.dumps({"section": args.section, args.section: res}), flush=True)
         return
     w = workload(args)

@@ -50,8 +50,11 @@ struct Contact {
   double nrm[3], delta, vr[3], meff, ri;
 };
 
-__device__ __forceinline__ void contact_law(const DemK& K, const Contact& ct, const double* xo, double* F, double* T,
-                                            double* xn) {
+// The contact law of one contact: its force term fn n + ft, its torque term r_i (n x ft) and the
+// new tangential spring.  The owner of the contact adds them in contact order: F += f, T -= t
+// (the operation order of the oracle's accumulation).
+__device__ __forceinline__ void contact_terms(const DemK& K, const Contact& ct, const double* xo, double* f, double* t,
+                                              double* xn) {
   const double* n = ct.nrm;
   const double vn = dadd(dadd(dmul(ct.vr[0], n[0]), dmul(ct.vr[1], n[1])), dmul(ct.vr[2], n[2]));
   double vt[3];
@@ -76,13 +79,87 @@ __device__ __forceinline__ void contact_law(const DemK& K, const Contact& ct, co
     }
   }
 #pragma unroll
-  for (int c = 0; c < 3; ++c) F[c] = dadd(F[c], dadd(dmul(fn, n[c]), ft[c]));
+  for (int c = 0; c < 3; ++c) f[c] = dadd(dmul(fn, n[c]), ft[c]);
   double nxf[3];
   cross3(n, ft, nxf);
 #pragma unroll
-  for (int c = 0; c < 3; ++c) T[c] = dsub(T[c], dmul(ct.ri, nxf[c]));
+  for (int c = 0; c < 3; ++c) t[c] = dmul(ct.ri, nxf[c]);
 #pragma unroll
   for (int c = 0; c < 3; ++c) xn[c] = xi[c];
+}
+
+// One sphere's state as the contact geometry needs it.
+struct DemSelf {
+  double x[3], v[3], w[3], r, m;
+};
+
+__device__ __forceinline__ DemSelf dem_self(const DemArgs& a, uint32_t k) {
+  const double4_32a A = a.sA[k], B = a.sB[k], W = a.sW[k];
+  DemSelf me;
+  me.x[0] = A.x; me.x[1] = A.y; me.x[2] = A.z; me.r = A.w;
+  me.v[0] = B.x; me.v[1] = B.y; me.v[2] = B.z; me.m = B.w;
+  me.w[0] = W.x; me.w[1] = W.y; me.w[2] = W.z;
+  return me;
+}
+
+// Geometry of a collected contact of `me`: code = the partner's sorted slot, or kWallId + face.
+// Sets the contact and the history key (the partner's id, or the wall code).
+__device__ __forceinline__ void contact_geometry(const DemArgs& a, const DemK& K, const DemSelf& me, uint32_t code,
+                                                 Contact& ct, uint32_t& pid) {
+  ct.ri = me.r;
+  if (code < kWallId) {
+    const uint32_t t = code;
+    pid = a.sorted_id[t];
+    const double4_32a Aj = a.sA[t], Bj = a.sB[t], Wj = a.sW[t];
+    const double d[3] = {dsub(me.x[0], Aj.x), dsub(me.x[1], Aj.y), dsub(me.x[2], Aj.z)};
+    const double d2 = dadd(dadd(dmul(d[0], d[0]), dmul(d[1], d[1])), dmul(d[2], d[2]));
+    const double rs = dadd(me.r, Aj.w);
+    const double dist = __dsqrt_rn(d2);
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) ct.nrm[cc] = ddiv(d[cc], dist);
+    ct.delta = dsub(rs, dist);
+    const double wj[3] = {Wj.x, Wj.y, Wj.z};
+    const double vj[3] = {Bj.x, Bj.y, Bj.z};
+    double ws[3], cr[3];
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) ws[cc] = dadd(dmul(me.r, me.w[cc]), dmul(Aj.w, wj[cc]));
+    cross3(ws, ct.nrm, cr);
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) ct.vr[cc] = dsub(dsub(me.v[cc], vj[cc]), cr[cc]);
+    const double mj = Bj.w;
+    ct.meff = ddiv(dmul(me.m, mj), dadd(me.m, mj));
+  } else {
+    const int face = (int)(code - kWallId);
+    const int ax = face / 2;
+    const bool hi_face = face & 1;
+    const double dist = hi_face ? dsub(K.wall_hi[ax], me.x[ax]) : dsub(me.x[ax], K.wall_lo[ax]);
+    pid = code;
+    ct.nrm[0] = ct.nrm[1] = ct.nrm[2] = 0.0;
+    ct.nrm[ax] = hi_face ? -1.0 : 1.0;
+    ct.delta = dsub(me.r, dist);
+    double ws[3], cr[3];
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) ws[cc] = dmul(me.r, me.w[cc]);
+    cross3(ws, ct.nrm, cr);
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) ct.vr[cc] = dsub(me.v[cc], cr[cc]);
+    ct.meff = me.m;
+  }
+}
+
+// Tangential spring of partner `pid` in a history row (zero if the pair was not in contact).
+__device__ __forceinline__ void history_lookup(const uint32_t* hp, const double* hx, int C, uint32_t pid, double* out) {
+  out[0] = out[1] = out[2] = 0.0;
+  for (int s = 0; s < C; ++s) {
+    const uint32_t q = hp[s];
+    if (q == kNoPartner) break;
+    if (q == pid) {
+      out[0] = hx[s * 3];
+      out[1] = hx[s * 3 + 1];
+      out[2] = hx[s * 3 + 2];
+      break;
+    }
+  }
 }
 
 __global__ void dem_gather_kernel(DemArgs a) {
@@ -118,118 +195,82 @@ __device__ __noinline__ D3 spin_update(D3 w, D3 T, double I, double dt) {
   return r;
 }
 
-// Contacts a thread collects during its candidate walk before it evaluates them.  The walk
-// only tests (FP32 screen, then the exact f64 test); the contact law runs afterwards for the
-// collected contacts, in the order they were found, so the lanes of a warp evaluate their q-th
-// contacts together.  Evaluated inline, each lane's contact ran alone while the others waited
-// (a few contacts per particle among about 200 candidates, at different iterations per lane).
+// Contacts a thread collects during its candidate walk before they are evaluated.  The walk
+// only tests (FP32 screen, then the exact f64 test).  The contact law then runs for the
+// contacts of the whole warp together: the warp's contacts are numbered in (lane, order found)
+// order and each lane evaluates one contact of a chunk of 32, whichever particle owns it; each
+// owner then adds the terms of its own contacts in the order it found them, so the sums and the
+// history are the oracle's, bit for bit.  Evaluated in the walk, each lane's contact ran alone
+// while the others waited (a few contacts per particle among about 200 candidates, at different
+// iterations per lane); evaluated per lane after the walk, a warp ran as many rounds as its
+// busiest lane had contacts.  A lane that collects more than kDemBuf contacts evaluates the
+// first kDemBuf itself, in order, before walking on (rare).
 constexpr int kDemThreads = 128;
+constexpr int kDemWarps = kDemThreads / 32;
 constexpr int kDemBuf = 16;
 
+struct DemTerm {  // results of one evaluated contact, for its owner
+  double f[3], t[3], xn[3];
+  uint32_t pid;
+};
+
 __global__ void __launch_bounds__(kDemThreads) dem_pass_kernel(DemArgs a) {
-  __shared__ uint32_t s_buf[kDemBuf][kDemThreads];  // [q][thread]: slot of a partner, or kWallId + face
-  const int tid = threadIdx.x;
+  __shared__ uint32_t s_buf[kDemBuf][kDemThreads];   // [q][thread]: slot of a partner, or kWallId + face
+  __shared__ uint16_t s_owner[kDemWarps][32 * kDemBuf];  // warp contact c -> (owner lane << 8) | q
+  __shared__ DemTerm s_term[kDemWarps][32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t k = blockIdx.x * blockDim.x + tid;
+  const bool live = k < a.n;
+  const DemK& K = a.K[0];
+  const int C = K.capacity;
   unsigned long long my_contacts = 0;
-  if (k < a.n) {
-    const DemK& K = a.K[0];
-    const int C = K.capacity;
-    const uint32_t id = a.sorted_id[k];
-    const double4_32a Ai = a.sA[k], Bi = a.sB[k], Wi = a.sW[k];
-    const double xi[3] = {Ai.x, Ai.y, Ai.z};
-    const double vi[3] = {Bi.x, Bi.y, Bi.z};
-    const double wi[3] = {Wi.x, Wi.y, Wi.z};
-    const double ri = Ai.w, mi = Bi.w;
+  const uint32_t id = live ? a.sorted_id[k] : 0u;
+  const DemSelf me = dem_self(a, live ? k : 0u);
+  uint32_t* hp_new = a.hpid_new + (size_t)id * C;
+  double* hx_new = a.hxi_new + (size_t)id * C * 3;
+  double F[3] = {0, 0, 0}, T[3] = {0, 0, 0};
+  int slot = 0;
+  bool overflow = false;
+  int nbuf = 0;
+
+  auto store = [&](uint32_t pid, const double* xv) {
+    if (slot < C) {
+      hp_new[slot] = pid;
+      hx_new[slot * 3] = xv[0];
+      hx_new[slot * 3 + 1] = xv[1];
+      hx_new[slot * 3 + 2] = xv[2];
+      ++slot;
+    } else {
+      overflow = true;
+    }
+  };
+  auto add_terms = [&](const double* f, const double* t) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) F[c] = dadd(F[c], f[c]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) T[c] = dsub(T[c], t[c]);
+  };
+
+  if (live) {
     const uint32_t* hp_old = a.hpid_old + (size_t)id * C;
     const double* hx_old = a.hxi_old + (size_t)id * C * 3;
-    uint32_t* hp_new = a.hpid_new + (size_t)id * C;
-    double* hx_new = a.hxi_new + (size_t)id * C * 3;
-    double F[3] = {0, 0, 0}, T[3] = {0, 0, 0};
-    int slot = 0;
-    bool overflow = false;
-
-    auto lookup = [&](uint32_t pid, double* out) {
-      out[0] = out[1] = out[2] = 0.0;
-      for (int s = 0; s < C; ++s) {
-        const uint32_t q = hp_old[s];
-        if (q == kNoPartner) break;
-        if (q == pid) {
-          out[0] = hx_old[s * 3];
-          out[1] = hx_old[s * 3 + 1];
-          out[2] = hx_old[s * 3 + 2];
-          break;
-        }
-      }
-    };
-    auto store = [&](uint32_t pid, const double* xv) {
-      if (slot < C) {
-        hp_new[slot] = pid;
-        hx_new[slot * 3] = xv[0];
-        hx_new[slot * 3 + 1] = xv[1];
-        hx_new[slot * 3 + 2] = xv[2];
-        ++slot;
-      } else {
-        overflow = true;
-      }
-    };
-
-    // Evaluate the collected contacts in the order found: the geometry of a particle or wall
-    // contact, then the history lookup, the contact law and the history store, shared by both.
-    int nbuf = 0;
-    auto flush = [&]() {
+    // the lane's own evaluation of its buffer (only when it fills during the walk)
+    auto flush_own = [&]() {
       for (int q = 0; q < nbuf; ++q) {
-        const uint32_t code = s_buf[q][tid];
         Contact ct;
         uint32_t pid;
-        ct.ri = ri;
-        if (code < kWallId) {
-          const uint32_t t = code;
-          pid = a.sorted_id[t];
-          const double4_32a Aj = a.sA[t], Bj = a.sB[t], Wj = a.sW[t];
-          const double d[3] = {dsub(xi[0], Aj.x), dsub(xi[1], Aj.y), dsub(xi[2], Aj.z)};
-          const double d2 = dadd(dadd(dmul(d[0], d[0]), dmul(d[1], d[1])), dmul(d[2], d[2]));
-          const double rs = dadd(ri, Aj.w);
-          const double dist = __dsqrt_rn(d2);
-#pragma unroll
-          for (int cc = 0; cc < 3; ++cc) ct.nrm[cc] = ddiv(d[cc], dist);
-          ct.delta = dsub(rs, dist);
-          const double wj[3] = {Wj.x, Wj.y, Wj.z};
-          const double vj[3] = {Bj.x, Bj.y, Bj.z};
-          double ws[3], cr[3];
-#pragma unroll
-          for (int cc = 0; cc < 3; ++cc) ws[cc] = dadd(dmul(ri, wi[cc]), dmul(Aj.w, wj[cc]));
-          cross3(ws, ct.nrm, cr);
-#pragma unroll
-          for (int cc = 0; cc < 3; ++cc) ct.vr[cc] = dsub(dsub(vi[cc], vj[cc]), cr[cc]);
-          const double mj = Bj.w;
-          ct.meff = ddiv(dmul(mi, mj), dadd(mi, mj));
-        } else {
-          const int face = (int)(code - kWallId);
-          const int ax = face / 2;
-          const bool hi_face = face & 1;
-          const double dist = hi_face ? dsub(K.wall_hi[ax], xi[ax]) : dsub(xi[ax], K.wall_lo[ax]);
-          pid = code;
-          ct.nrm[0] = ct.nrm[1] = ct.nrm[2] = 0.0;
-          ct.nrm[ax] = hi_face ? -1.0 : 1.0;
-          ct.delta = dsub(ri, dist);
-          double ws[3], cr[3];
-#pragma unroll
-          for (int cc = 0; cc < 3; ++cc) ws[cc] = dmul(ri, wi[cc]);
-          cross3(ws, ct.nrm, cr);
-#pragma unroll
-          for (int cc = 0; cc < 3; ++cc) ct.vr[cc] = dsub(vi[cc], cr[cc]);
-          ct.meff = mi;
-        }
-        double xo[3], xn[3];
-        lookup(pid, xo);
-        contact_law(K, ct, xo, F, T, xn);
+        contact_geometry(a, K, me, s_buf[q][tid], ct, pid);
+        double xo[3], f[3], t[3], xn[3];
+        history_lookup(hp_old, hx_old, C, pid, xo);
+        contact_terms(K, ct, xo, f, t, xn);
+        add_terms(f, t);
         store(pid, xn);
       }
       nbuf = 0;
     };
     auto collect = [&](uint32_t code) {
       s_buf[nbuf][tid] = code;
-      if (++nbuf == kDemBuf) flush();  // rare: more contacts than the buffer holds
+      if (++nbuf == kDemBuf) flush_own();
     };
 
     // FP32 prefilter: |x_i - x_j| < r_i + r_j in f64  =>  the FP32 r^2 below is < thr_j
@@ -271,9 +312,9 @@ __global__ void __launch_bounds__(kDemThreads) dem_pass_kernel(DemArgs a) {
         }
         if (t == k) continue;  // the particle itself (slot k holds id)
         const double4_32a Aj = a.sA[t];
-        const double d[3] = {dsub(xi[0], Aj.x), dsub(xi[1], Aj.y), dsub(xi[2], Aj.z)};
+        const double d[3] = {dsub(me.x[0], Aj.x), dsub(me.x[1], Aj.y), dsub(me.x[2], Aj.z)};
         const double d2 = dadd(dadd(dmul(d[0], d[0]), dmul(d[1], d[1])), dmul(d[2], d[2]));
-        const double rs = dadd(ri, Aj.w);
+        const double rs = dadd(me.r, Aj.w);
         if (!(d2 < dmul(rs, rs))) continue;
         collect(t);
         ++my_contacts;
@@ -291,11 +332,53 @@ __global__ void __launch_bounds__(kDemThreads) dem_pass_kernel(DemArgs a) {
         const float wslack = 2.384185791015625e-07f * (2.f * (fabsf(xf) + fabsf(wf)) + fi.w) + 1.0e-6f * fi.w;
         if (df >= fi.w + wslack) continue;
       }
-      const double dist = hi_face ? dsub(K.wall_hi[ax], xi[ax]) : dsub(xi[ax], K.wall_lo[ax]);
-      if (!(dist < ri)) continue;
+      const double dist = hi_face ? dsub(K.wall_hi[ax], me.x[ax]) : dsub(me.x[ax], K.wall_lo[ax]);
+      if (!(dist < me.r)) continue;
       collect(kWallId + (uint32_t)face);
     }
-    flush();  // the lanes of a warp evaluate their collected contacts together
+  }
+
+  // ---- the warp's collected contacts, 32 at a time, one per lane (every lane of the warp
+  // takes part: lanes without a particle have none) ----
+  int first = nbuf;  // exclusive prefix of the lanes' counts = number of the lane's first contact
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, first, off);
+    if (lane >= off) first += v;
+  }
+  const int total = __shfl_sync(0xffffffffu, first, 31);
+  first -= nbuf;
+  for (int q = 0; q < nbuf; ++q) s_owner[warp][first + q] = (uint16_t)((lane << 8) | q);
+  __syncwarp();
+  for (int c0 = 0; c0 < total; c0 += 32) {
+    const int c = c0 + lane;
+    if (c < total) {
+      const int own = s_owner[warp][c];
+      const int ol = own >> 8, oq = own & 0xff;
+      const uint32_t ok = k - (uint32_t)lane + (uint32_t)ol;  // the owner's slot
+      const uint32_t oid = a.sorted_id[ok];
+      const DemSelf om = dem_self(a, ok);
+      Contact ct;
+      uint32_t pid;
+      contact_geometry(a, K, om, s_buf[oq][warp * 32 + ol], ct, pid);
+      double xo[3];
+      history_lookup(a.hpid_old + (size_t)oid * C, a.hxi_old + (size_t)oid * C * 3, C, pid, xo);
+      DemTerm& r = s_term[warp][lane];
+      contact_terms(K, ct, xo, r.f, r.t, r.xn);
+      r.pid = pid;
+    }
+    __syncwarp();
+    // each owner adds its contacts of this chunk, in order
+    const int lo = max(first, c0), hi = min(first + nbuf, c0 + 32);
+    for (int cc = lo; cc < hi; ++cc) {
+      const DemTerm& r = s_term[warp][cc - c0];
+      add_terms(r.f, r.t);
+      store(r.pid, r.xn);
+    }
+    __syncwarp();
+  }
+
+  if (live) {
     // Slots after the last contact must read as empty.  The buffer being written held this
     // particle's history of two steps ago, and every history buffer is empty after its first
     // empty slot (initial state, pg_dem_set_history and this loop keep that), so only the
@@ -317,29 +400,29 @@ __global__ void __launch_bounds__(kDemThreads) dem_pass_kernel(DemArgs a) {
     // with a finite dt, w' = w + dt * (+-0) is w itself unless w is +-0 (then it is computed).
     const size_t o = (size_t)id * 3;
     const bool free_t = is_zero(T[0]) && is_zero(T[1]) && is_zero(T[2]);
-    const double I = free_t ? 0.0 : dmul(dmul(dmul(0.4, mi), ri), ri);
-    const bool m_ok = positive_finite(mi);
+    const double I = free_t ? 0.0 : dmul(dmul(dmul(0.4, me.m), me.r), me.r);
+    const bool m_ok = positive_finite(me.m);
     // F / m: the divisions sit behind a branch that the particles without a contact force skip
     // (a select would run them for every particle: the f64 division is a sequence of DFMAs)
     double fm[3] = {F[0], F[1], F[2]};
     if (!(m_ok && is_zero(F[0]) && is_zero(F[1]) && is_zero(F[2]))) {
-      const D3 q = force_per_mass(D3{F[0], F[1], F[2]}, mi, m_ok);
+      const D3 q = force_per_mass(D3{F[0], F[1], F[2]}, me.m, m_ok);
       fm[0] = q.x;
       fm[1] = q.y;
       fm[2] = q.z;
     }
 #pragma unroll
     for (int cc = 0; cc < 3; ++cc) {
-      const double v = dadd(vi[cc], dmul(K.dt, dadd(fm[cc], K.grav[cc])));
+      const double v = dadd(me.v[cc], dmul(K.dt, dadd(fm[cc], K.grav[cc])));
       a.vel[o + cc] = v;
-      a.pos[o + cc] = dadd(xi[cc], dmul(K.dt, v));
+      a.pos[o + cc] = dadd(me.x[cc], dmul(K.dt, v));
     }
-    if (free_t && K.dt_finite && positive_finite(dmul(dmul(dmul(0.4, mi), ri), ri))) {
+    if (free_t && K.dt_finite && positive_finite(dmul(dmul(dmul(0.4, me.m), me.r), me.r))) {
 #pragma unroll
       for (int cc = 0; cc < 3; ++cc)
-        a.omega[o + cc] = is_zero(wi[cc]) ? dadd(wi[cc], dmul(K.dt, T[cc])) : wi[cc];
+        a.omega[o + cc] = is_zero(me.w[cc]) ? dadd(me.w[cc], dmul(K.dt, T[cc])) : me.w[cc];
     } else {
-      const D3 w = spin_update(D3{wi[0], wi[1], wi[2]}, D3{T[0], T[1], T[2]}, I, K.dt);
+      const D3 w = spin_update(D3{me.w[0], me.w[1], me.w[2]}, D3{T[0], T[1], T[2]}, I, K.dt);
       a.omega[o] = w.x;
       a.omega[o + 1] = w.y;
       a.omega[o + 2] = w.z;
