@@ -29,6 +29,7 @@ Multi-GPU (torchrun): every rank runs an independent replica of the workload on 
 particle-steps / the slowest rank's time.
 """
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -48,15 +49,13 @@ MOM_BYTES = {"f64": 112, "f32": 56}
 # Algorithmic bytes per particle-step of the DEM contact pass with its fused integrator: reads
 # pos, vel, omega (72 B), radius and mass (16 B); writes pos, vel, omega (72 B).
 DEM_BYTES = 160
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per particle of one momentum-pass
-# launch (sph_list_pass_kernel, SPH_MOM) in an ncu capture at 1,000,000 particles (f64
-# double-word mode), scaled by the particle count.  Most of it is the per-entry
-# cache the continuity pass writes for it (16 B per neighbour) and the neighbour lists (4 B per
-# neighbour): the pass reads cached pair terms instead of recomputing them.
-MOM_TRAFFIC_PER_PARTICLE = {"f64-fast": 1739.0}
-# The resource that binds the momentum pass in that capture: FMA-pipe cycles active (% of peak,
-# sm__pipe_fma_cycles_active) and issue slots active (smsp__issue_active).
-MOM_PIPES = {"f64-fast": {"fma_pipe_active_pct": 50.9, "issue_active_pct": 68.7}}
+# The momentum pass's ncu figures (DRAM bytes per particle of one launch, FMA-pipe and issue
+# activity) from a capture at 1,000,000 particles, f64 double-word mode, with the command that
+# made it and a digest of the pass's sources at the time; the bench line scales the bytes by the
+# particle count and says whether the digest matches the sources being run.
+MOM_PROFILE = os.path.join(ROOT, "profiles", "momentum_pass_lattice1m.json")
+PASS_SOURCES = ("prestige_gb300/csrc/pg_sph.cu", "prestige_gb300/csrc/pg_sph_pass.cuh",
+                "prestige_gb300/csrc/pg_arith.cuh")
 
 # Flops of the method (each +, -, *, / and sqrt of the oracle's f64 step one flop), counted by the
 # oracle's flop census on the 110,592-particle lattice of the same construction (seed 2):
@@ -261,6 +260,26 @@ def run_reference(args, rank, world, pgroup):
            "cpu_baseline": cpu_record(value, threads, sample),
            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+def sources_digest(paths=PASS_SOURCES):
+    h = hashlib.sha256()
+    for p in paths:
+        with open(os.path.join(ROOT, p), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def momentum_profile():
+    """The committed ncu figures of the momentum pass, and whether they were captured from the
+    sources being run."""
+    try:
+        with open(MOM_PROFILE) as f:
+            d = json.load(f)
+    except (OSError, ValueError):
+        return None
+    d["matches_sources"] = d.get("sources_digest") == sources_digest()
+    return d
 
 
 def _peak_hbm():
@@ -576,8 +595,8 @@ def run_gpu(args, rank, world, local, pgroup):
     bpp = MOM_BYTES[args.precision]
     achieved = bpp * n / (mom_ms * 1e-3) / 1e9
     peak, peak_src = _peak_hbm()
-    tpp = MOM_TRAFFIC_PER_PARTICLE.get("%s-%s" % (args.precision, args.mode))
-    traffic = tpp * n if tpp else None
+    prof = momentum_profile() if (args.precision, args.mode) == ("f64", "fast") else None
+    traffic = prof["dram_bytes_per_particle"] * n if prof else None
     # neighbour pairs per particle from the lists of the last timed step (lengths only)
     pairs = float(s.pair_counts().mean())
     exact_lists = args.precision == "f64" and args.mode == "fast"
@@ -646,11 +665,16 @@ def run_gpu(args, rank, world, local, pgroup):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "sph_list_pass_kernel (momentum pass)", "peak_source": peak_src,
-                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one momentum-pass "
-                                           "launch at 1,000,000 particles (1,739 B per particle: the per-entry cache and the lists), scaled by N"
-                         if traffic else None,
+                         "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one momentum-pass "
+                                            "launch at 1,000,000 particles (%.0f B per particle: mostly the per-entry "
+                                            "cache and the lists), scaled by N; %s; captured with: %s"
+                                            % (prof["dram_bytes_per_particle"],
+                                               "captured from the sources being run" if prof["matches_sources"]
+                                               else "STALE: the pass's sources changed since the capture",
+                                               prof["command"])) if prof else None,
                          "bytes_per_particle": bpp,
-                         "pipes_ncu": MOM_PIPES.get("%s-%s" % (args.precision, args.mode)),
+                         "pipes_ncu": {k: prof[k] for k in ("fma_pipe_active_pct", "issue_active_pct",
+                                                            "long_scoreboard_stalls_per_issue")} if prof else None,
                          "binding_resource": "FP32 issue (double-word f64 arithmetic) and the latency of the "
                                              "per-entry cache and record loads" if args.mode == "fast"
                          and args.precision == "f64" else ("FP64 pipe" if args.precision == "f64" else "FP32 issue")},
