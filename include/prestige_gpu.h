@@ -232,6 +232,17 @@ int pg_step(pg_system* sys, int nsteps);
 int pg_step_async(pg_system* sys, int nsteps);
 int pg_sync(pg_system* sys);
 
+/* One SPH step in two calls, for hosts that exchange densities between the two passes (a
+ * domain split across GPUs, whose halo particles take their densities from the GPU that owns
+ * them).  Stage 0: neighbour search, continuity pass, rho' = rho + dt drho into "rho".  Between
+ * the stages the caller may replace any densities (pg_set_field or pg_set_field_async of "rho").
+ * Stage 1: the packed densities and Tait pressures are refreshed from "rho", then the momentum
+ * pass updates v and x.  Stage 0 then stage 1 with nothing in between gives the same bits as
+ * pg_step(sys, 1).  PG_ESTATE if stage 1 does not follow a stage 0, or if a step, a neighbour
+ * search or a change of another field came in between.  Both calls wait for their work.  No
+ * reference counterpart (the reference's loop runs on one set of slices). */
+int pg_step_stage(pg_system* sys, int stage);
+
 /* Capture one full step as a CUDA graph; later steps replay it (same results). */
 int pg_enable_graph(pg_system* sys, int enable);
 

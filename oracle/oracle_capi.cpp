@@ -201,6 +201,66 @@ extern "C" double orc_sph_run(const orc_sph_spec* sp, int f64, long long n, void
   return run_t<float>(sp, (size_t)n, state, nsteps);
 }
 
+// Half of sph_step (prestige_oracle.hpp) on a state: stage 0 = the continuity pass, rho' into
+// rho; stage 1 = the momentum pass with the densities in rho (as rho') and the update of the
+// fluid's v and x.  Positions do not change between the stages, so both build the same cell list.
+template <class T, int DIM>
+static void stage_dim(const SphSpec& spec, const SphConst<T>& k, SphState<T>& s, int stage) {
+  CellList cl;
+  cl.g = make_grid(DIM, spec.lo, spec.hi, 2.0 * spec.h, spec.cell_mult);
+  const T* pos[3] = {s.x[0].data(), s.x[1].data(), DIM == 3 ? s.x[2].data() : s.x[0].data()};
+  build_cell_list<T>(cl, s.n, pos);
+  std::vector<T> P(s.n);
+  if (stage == 0) {
+    std::vector<T> rho_new(s.n);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long long i = 0; i < (long long)s.n; ++i) {
+      T a[3], dr;
+      sph_pair_loop<T, DIM, true, false>(cl, s, k, P, (size_t)i, a, dr);
+      rho_new[i] = s.rho[i] + k.dt * dr;
+    }
+    s.rho.swap(rho_new);
+    return;
+  }
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < (long long)s.n; ++i) P[i] = tait_pterm(k, s.rho[i]);
+  std::vector<T> acc[3];
+  for (int c = 0; c < DIM; ++c) acc[c].resize(s.n);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long i = 0; i < (long long)s.n; ++i) {
+    T a[3], dr;
+    sph_pair_loop<T, DIM, false, true>(cl, s, k, P, (size_t)i, a, dr);
+    for (int c = 0; c < DIM; ++c) acc[c][i] = a[c];
+  }
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < (long long)s.n; ++i) {
+    if ((size_t)i < spec.n_fluid) {
+      for (int c = 0; c < DIM; ++c) {
+        s.v[c][i] = s.v[c][i] + k.dt * (acc[c][i] + k.g[c]);
+        s.x[c][i] = s.x[c][i] + k.dt * s.v[c][i];
+      }
+    }
+  }
+}
+
+template <class T>
+static void stage_t(const orc_sph_spec* sp, size_t n, void* const* state, int stage) {
+  SphSpec spec = to_spec(sp);
+  SphState<T> s;
+  load_state<T>(s, spec.dim, n, (T* const*)state);
+  SphConst<T> k = sph_consts<T>(spec, T(spec.alpha), T(spec.B));
+  if (spec.dim == 2) stage_dim<T, 2>(spec, k, s, stage);
+  else stage_dim<T, 3>(spec, k, s, stage);
+  store_state<T>(s, spec.dim, n, (T* const*)state);
+}
+
+extern "C" int orc_sph_stage(const orc_sph_spec* sp, int f64, long long n, void* const* state, int stage) {
+  if (stage != 0 && stage != 1) return 1;
+  if (f64) stage_t<double>(sp, (size_t)n, state, stage);
+  else stage_t<float>(sp, (size_t)n, state, stage);
+  return 0;
+}
+
 // Flop census of one SPH step on a double state (not modified), counted on one thread.
 // out: particles, candidates, pairs, continuity-loop flops, momentum-loop flops, step flops,
 // flops of one candidate test.

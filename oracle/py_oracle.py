@@ -227,6 +227,16 @@ def sph_run_timing(cfg, state, nsteps):
                                             state.ptrs(), int(nsteps))
 
 
+def sph_stage(cfg, state, stage):
+    """Half of an oracle step, in place: 0 = continuity (rho' into rho), 1 = momentum with the
+    densities in rho and the update of the fluid's velocities and positions."""
+    spec = sph_spec(cfg, state.n)
+    rc = load().orc_sph_stage(ctypes.byref(spec), 1 if state.f64 else 0, ctypes.c_longlong(state.n),
+                              state.ptrs(), int(stage))
+    if rc:
+        raise ValueError("stage must be 0 or 1")
+
+
 def sph_flop_census(cfg, state):
     """Counted flops of one oracle SPH step on `state` (f64, not modified): a dict with the
     particle, candidate and neighbour-pair counts, the flops of the continuity and momentum pair

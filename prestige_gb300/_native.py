@@ -96,6 +96,7 @@ SIGNATURES = {
     "pg_set_tuning": (_I, [_P, _I, ctypes.c_double, _I]),
     "pg_set_momentum_block": (_I, [_P, _I]),
     "pg_set_particles_per_warp": (_I, [_P, _I]),
+    "pg_step_stage": (_I, [_P, _I]),
     "pg_measure_fma_peaks": (_I, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "pg_timing_enable": (_I, [_P, _I]),
     "pg_timing_read": (_I, [_P, ctypes.POINTER(PgTiming)]),

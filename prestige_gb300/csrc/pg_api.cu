@@ -207,6 +207,7 @@ NbrArgs nbr_args(pg_system* s) {
 
 // Hash + stable sort + cell table for the current positions (enqueued on the stream).
 int enqueue_neighbors(pg_system* s) {
+  s->stage_pending = false;  // any neighbour search ends a pending pg_step_stage(0)
   const void* pos = s->pos.p;
   // the double-word packs need the step's minimum position (sph_gather_df)
   unsigned long long* posmin = nullptr;
@@ -225,16 +226,18 @@ int mom_block(const pg_system* s) { return s->block_mom > 0 ? s->block_mom : s->
 // Kernels enqueued by one neighbour search (hash, radix passes, cell count, scan).
 long long neighbor_launches(const pg_system* s) { return 1 + 3LL * s->nw.passes + 1 + (s->ncells ? 3 : 0); }
 
-// ev (optional): 6 events recorded at stage boundaries (start, after the neighbour search,
-// after the sorted gather, after the neighbour lists, after the continuity pass, end).
-int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
+// The continuity part of a step: neighbour search, sorted gather, neighbour lists and the
+// continuity pass (rho' into the canonical density and the sorted pack).  ev (optional): events
+// 0-4 of a step (start, after the neighbour search, after the sorted gather, after the lists,
+// after the continuity pass).
+int enqueue_sph_front(pg_system* s, cudaEvent_t* ev) {
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[0], s->stream));
   PG_TRY(enqueue_neighbors(s));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[1], s->stream));
-  SphArgs a = sph_args(s, integrate, rates);
+  SphArgs a = sph_args(s, 1, false);
   PG_TRY(launch_sph_gather(s->stream, a, s->arith));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[2], s->stream));
-  if (!rates && s->ov_split > 0 && s->ov_split < s->n) {
+  if (s->ov_split > 0 && s->ov_split < s->n) {
     // lists of [0, split) first; then the continuity pass over them runs beside the lists of
     // [split, n) on the auxiliary stream, which goes on with the continuity pass over
     // [split, n) (neither continuity launch reads the packed rho' the other writes); the
@@ -253,24 +256,47 @@ int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
     PG_TRY(launch_sph_list_pass(s->stream, a1, s->arith, SPH_CONT, s->ov_pass_grid, s->block, s->lanes));
     PG_CUDA_TRY(cudaStreamWaitEvent(s->stream, s->ov_ev[1], 0));
     if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
-    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], mom_block(s), s->lanes));
-    s->launches += neighbor_launches(s) + 6;
-    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[5], s->stream));
+    s->launches += neighbor_launches(s) + 5;
     return PG_OK;
   }
   PG_TRY(launch_sph_list(s->stream, a, s->arith, s->list_grid, s->block));
   s->list_arith = s->arith;
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
-  if (rates) {
-    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_RATES, s->pass_grid[SPH_RATES], s->block));
-    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
-    s->launches += neighbor_launches(s) + 3;
-  } else {
-    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_CONT, s->pass_grid[SPH_CONT], s->block, s->lanes));
-    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
-    PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], mom_block(s), s->lanes));
-    s->launches += neighbor_launches(s) + 4;
+  PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_CONT, s->pass_grid[SPH_CONT], s->block, s->lanes));
+  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
+  s->launches += neighbor_launches(s) + 3;
+  return PG_OK;
+}
+
+// The momentum part of a step: the momentum pass with the packed rho' (velocity and position
+// update).  ev (optional): event 5 of a step (end).
+int enqueue_sph_momentum(pg_system* s, cudaEvent_t* ev) {
+  SphArgs a = sph_args(s, 1, false);
+  PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], mom_block(s), s->lanes));
+  s->launches += 1;
+  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[5], s->stream));
+  return PG_OK;
+}
+
+// ev (optional): 6 events recorded at stage boundaries (start, after the neighbour search,
+// after the sorted gather, after the neighbour lists, after the continuity pass, end).
+int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev) {
+  if (!rates) {
+    PG_TRY(enqueue_sph_front(s, ev));
+    return enqueue_sph_momentum(s, ev);
   }
+  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[0], s->stream));
+  PG_TRY(enqueue_neighbors(s));
+  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[1], s->stream));
+  SphArgs a = sph_args(s, integrate, rates);
+  PG_TRY(launch_sph_gather(s->stream, a, s->arith));
+  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[2], s->stream));
+  PG_TRY(launch_sph_list(s->stream, a, s->arith, s->list_grid, s->block));
+  s->list_arith = s->arith;
+  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
+  PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_RATES, s->pass_grid[SPH_RATES], s->block));
+  if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
+  s->launches += neighbor_launches(s) + 3;
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[5], s->stream));
   return PG_OK;
 }
@@ -951,6 +977,7 @@ int pg_set_field(pg_system* s, const char* name, const void* host, size_t count,
     pg::set_error("null name or buffer");
     return PG_EINVAL;
   }
+  if (strcmp(name, "rho") != 0) s->stage_pending = false;  // only densities may change between stages
   if (dtype != PG_F32 && dtype != PG_F64) {
     pg::set_error("dtype must be PG_F32 or PG_F64");
     return PG_EINVAL;
@@ -999,6 +1026,7 @@ int pg_set_field(pg_system* s, const char* name, const void* host, size_t count,
 
 int pg_set_field_async(pg_system* s, const char* name, const void* host, size_t count, int dtype) {
   PG_TRY(check(s));
+  if (name && strcmp(name, "rho") != 0) s->stage_pending = false;
   pg::DevBuf* b;
   size_t bytes;
   PG_TRY(io_field(s, name, host, count, dtype, true, &b, &bytes));
@@ -1260,6 +1288,35 @@ int pg_sync(pg_system* s) {
 
 int pg_step(pg_system* s, int nsteps) {
   PG_TRY(pg_step_async(s, nsteps));
+  return pg::sync_and_check(s);
+}
+
+int pg_step_stage(pg_system* s, int stage) {
+  PG_TRY(check(s));
+  if (s->model != PG_MODEL_SPH) {
+    pg::set_error("pg_step_stage is for SPH systems");
+    return PG_EINVAL;
+  }
+  if (stage == 0) {
+    PG_TRY(pg::enqueue_sph_front(s, nullptr));
+    s->nbr_valid = false;
+    PG_TRY(pg::sync_and_check(s));
+    s->stage_pending = true;
+    return PG_OK;
+  }
+  if (stage != 1) {
+    pg::set_error("stage must be 0 or 1 (got %d)", stage);
+    return PG_EINVAL;
+  }
+  if (!s->stage_pending) {
+    pg::set_error("pg_step_stage(1) needs pg_step_stage(0) first, with no other step, neighbour search or "
+                  "field change but rho in between");
+    return PG_ESTATE;
+  }
+  s->stage_pending = false;
+  SphArgs a = pg::sph_args(s, 1, false);
+  PG_TRY(pg::launch_sph_repack_rho(s->stream, a, s->arith));
+  PG_TRY(pg::enqueue_sph_momentum(s, nullptr));
   return pg::sync_and_check(s);
 }
 

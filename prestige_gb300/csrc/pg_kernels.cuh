@@ -91,6 +91,7 @@ struct SphArgs {
 };
 
 int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith);
+int launch_sph_repack_rho(cudaStream_t st, const SphArgs& a, int arith);  // packed rho', P' from rho
 // Neighbour lists for the list-based passes (stage passes read a.nlist / a.nlen / a.nresume).
 // block: threads per block (multiple of 32, <= kSphMaxThreads).
 int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid, int block);

@@ -105,6 +105,27 @@ __device__ __forceinline__ float4 df_pack_rho(const SphDF& w, int gamma, double 
   return r;
 }
 
+// The packed {rho', P'} of every slot from the canonical density, exactly as the continuity pass
+// packs them (pg_step_stage: the caller may replace densities between the two passes).
+template <class Ops>
+__global__ void sph_repack_rho_real(SphArgs a) {
+  typedef typename Ops::R R;
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.n) return;
+  const uint32_t id = a.sorted_id[k];
+  const SphK& K = a.sys[sys_of_slot(a, id)];
+  const R rn = ((const R*)a.rho)[id];
+  ((typename V2<R>::T*)a.s[2])[k] = make2<R>(rn, tait_pterm<Ops>(consts<R>(K), K.gamma, rn));
+}
+
+__global__ void sph_repack_rho_df(SphArgs a) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.n) return;
+  const uint32_t id = a.sorted_id[k];
+  const SphK& K = a.sys[sys_of_slot(a, id)];
+  ((float4*)a.s[4])[k] = df_pack_rho(K.w, K.gamma, ((const double*)a.rho)[id]);
+}
+
 // The pair passes' per-slot record in the double-word mode: positions and mass (hi, lo) and
 // velocities (hi, lo), 64 bytes, so the four loads of a neighbour touch two sectors of one line.
 struct __align__(64) DfRecord {
@@ -632,6 +653,22 @@ int launch_sph_gather(cudaStream_t st, const SphArgs& a, int arith) {
 int sph_pass_lanes(int arith, int stage, int lanes) {
   const bool tolerant = arith == ARITH_F64_DF || arith == ARITH_F32_FAST;
   return tolerant && (stage == SPH_CONT || stage == SPH_MOM) && (lanes == 2 || lanes == 4) ? lanes : 1;
+}
+
+int launch_sph_repack_rho(cudaStream_t st, const SphArgs& a, int arith) {
+  if (a.n == 0) return PG_OK;
+  const unsigned blocks = (a.n + 255) / 256;
+  switch (arith) {
+    case ARITH_F64_EXACT: sph_repack_rho_real<OpsD><<<blocks, 256, 0, st>>>(a); break;
+    case ARITH_F64_DF: sph_repack_rho_df<<<blocks, 256, 0, st>>>(a); break;
+    case ARITH_F32_EXACT: sph_repack_rho_real<OpsF><<<blocks, 256, 0, st>>>(a); break;
+    case ARITH_F32_FAST: sph_repack_rho_real<OpsFF><<<blocks, 256, 0, st>>>(a); break;
+    default:
+      set_error("unknown arithmetic mode %d", arith);
+      return PG_EINVAL;
+  }
+  PG_CUDA_TRY(cudaGetLastError());
+  return PG_OK;
 }
 
 int launch_sph_list(cudaStream_t st, const SphArgs& a, int arith, int grid, int block) {

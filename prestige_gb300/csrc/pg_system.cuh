@@ -44,6 +44,7 @@ struct pg_system {
   // neighbour search and sorted copies
   pg::NbrWork nw;
   bool nbr_valid = false;
+  bool stage_pending = false;  // pg_step_stage(0) ran; pg_step_stage(1) may follow
   pg::DevBuf sorted[6];
   pg::DevBuf spos;
   pg::DevBuf tmp, tmp2, tmp3, tmp4;
@@ -108,6 +109,8 @@ int ensure_sorted_buffers(pg_system* s);
 SphArgs sph_args(pg_system* s, int integrate, bool rates);
 int enqueue_neighbors(pg_system* s);
 int enqueue_sph_step(pg_system* s, bool rates, int integrate, cudaEvent_t* ev);
+int enqueue_sph_front(pg_system* s, cudaEvent_t* ev);
+int enqueue_sph_momentum(pg_system* s, cudaEvent_t* ev);
 long long neighbor_launches(const pg_system* s);
 int sync_and_check(pg_system* s);
 int choose_pass_grid(pg_system* s);

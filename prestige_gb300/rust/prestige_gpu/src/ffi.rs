@@ -144,6 +144,7 @@ extern "C" {
     pub fn pg_compute_rates(sys: *mut pg_system) -> c_int;
     pub fn pg_step(sys: *mut pg_system, nsteps: c_int) -> c_int;
     pub fn pg_step_async(sys: *mut pg_system, nsteps: c_int) -> c_int;
+    pub fn pg_step_stage(sys: *mut pg_system, stage: c_int) -> c_int;
     pub fn pg_sync(sys: *mut pg_system) -> c_int;
     pub fn pg_enable_graph(sys: *mut pg_system, enable: c_int) -> c_int;
 

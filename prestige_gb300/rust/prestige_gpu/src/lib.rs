@@ -282,6 +282,11 @@ impl System {
         check(unsafe { ffi::pg_step(self.raw, nsteps) })
     }
 
+    /// Half a step: 0 = continuity (rho' into "rho"), 1 = momentum with the densities in "rho".
+    pub fn step_stage(&mut self, stage: i32) -> Result<()> {
+        check(unsafe { ffi::pg_step_stage(self.raw, stage) })
+    }
+
     pub fn step_async(&mut self, nsteps: i32) -> Result<()> {
         check(unsafe { ffi::pg_step_async(self.raw, nsteps) })
     }

@@ -221,6 +221,11 @@ class ParticleSystem:
     def step(self, nsteps=1):
         nat.check(self._lib.pg_step(self._h, int(nsteps)), "pg_step")
 
+    def step_stage(self, stage):
+        """Half a step: 0 = neighbour search and continuity pass (rho' into "rho"), 1 = the
+        momentum pass with the densities in "rho" (which the caller may replace in between)."""
+        nat.check(self._lib.pg_step_stage(self._h, int(stage)), "pg_step_stage")
+
     def step_async(self, nsteps=1):
         nat.check(self._lib.pg_step_async(self._h, int(nsteps)), "pg_step_async")
 
