@@ -6,6 +6,9 @@
   * The 2D dam break at dx = 0.02 (5,000 fluid + 1,518 wall particles) for its 2,000 steps:
       IEEE f64 bit-exact against the oracle, compared every 200 steps so a failure names the
       step window.
+  * DEM at 200,000 spheres, bit-exact: the settling workload (graph-replayed) and the
+      contact-dense compressed lattice of the DEM bench.
+  * The 512 uneven dam breaks of the batched bench (6.1 M particles) in one handle, IEEE f64.
 
 The oracle runs these on all host threads (about 1 s per 4M-particle step on 16 cores).
 """
@@ -100,3 +103,68 @@ def test_dam_break_full_size_2000_steps_ieee_bit_exact(pg, oracle):
     assert np.array_equal(p0[nf:], p1[nf:])  # walls fixed
     assert p1[:nf, 0].max() > 1.2  # the front has advanced from x = 0.99 m
     s.close()
+
+
+def _dem_pair(oracle, w):
+    s = ParticleSystem(make_config(**w["config"]), w["n"])
+    workloads.load_into(s, w)
+    f = w["fields"]
+    st = oracle.DemState(f["pos"], f["vel"], f["omega"], f["radius"], f["mass"], w["config"]["contact_capacity"])
+    return s, st
+
+
+def _dem_equal(s, st):
+    assert np.array_equal(s.get("pos"), st.pos)
+    assert np.array_equal(s.get("vel"), st.vel)
+    assert np.array_equal(s.get("omega"), st.omega)
+    pid, xi = s.dem_history()
+    assert np.array_equal(pid.reshape(-1), st.hpid)
+    assert np.array_equal(xi.reshape(-1), st.hxi)
+
+
+def test_dem_settling_200k_bit_exact(pg, oracle):
+    """The 200,000-sphere settling workload (random sequential insertion), 20 steps, graph-replayed."""
+    w = workloads.dem_settling(200000)
+    s, st = _dem_pair(oracle, w)
+    s.enable_graph(True)
+    s.step(20)
+    oracle.dem_run(w["config"], st, 20)
+    _dem_equal(s, st)
+    s.close()
+
+
+def test_dem_dense_200k_bit_exact(pg, oracle):
+    """200,000 spheres on the compressed lattice of the DEM bench: about 500,000 contacts per step,
+    tangential history, Coulomb slip and walls, 6 steps."""
+    w = workloads.dem_compressed_lattice(nside=(50, 50, 80))
+    s, st = _dem_pair(oracle, w)
+    for _ in range(3):
+        s.step(2)
+        c, _ = oracle.dem_run(w["config"], st, 2)
+        assert c > 400000 and s.dem_contacts() == c
+        _dem_equal(s, st)
+    s.close()
+
+
+def test_batched_512_dam_breaks_bit_exact(pg, oracle):
+    """The 512 uneven dam breaks of the batched bench (6.1 M particles) in one handle, IEEE f64,
+    graph-replayed: every system equals the oracle run of that system alone after 2 steps."""
+    systems = workloads.batched_dam_breaks()
+    assert len(systems) == 512
+    cfgs = [dict(w["config"], f64_mode=0) for w in systems]
+    b = ParticleSystem.batch(cfgs, [w["n"] for w in systems])
+    for k in ("pos", "vel", "rho", "mass"):
+        b.set(k, np.concatenate([w["fields"][k] for w in systems]))
+    b.enable_graph(True)
+    b.step(2)
+    pos, vel, rho = b.get("pos"), b.get("vel"), b.get("rho")
+    o = 0
+    for w in systems:
+        f = w["fields"]
+        st = oracle.SphState(f["pos"], f["vel"], f["rho"], f["mass"])
+        oracle.sph_run(w["config"], st, 2)
+        n = w["n"]
+        assert np.array_equal(pos[o:o + n], st.pos) and np.array_equal(vel[o:o + n], st.vel)
+        assert np.array_equal(rho[o:o + n], st.rho)
+        o += n
+    b.close()
