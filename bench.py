@@ -90,8 +90,9 @@ def parse():
     p.add_argument("--mom-block", type=int, default=0, help="momentum-pass block size used with --block (0: --block)")
     p.add_argument("--ppw", type=int, default=32, help="particles per warp of the pair passes used with --block")
     p.add_argument("--section", default="all",
-                   choices=["all", "batched", "adjoint", "dem", "dem_dense", "sweep", "drift"],
+                   choices=["all", "batched", "adjoint", "dem", "dem_settling", "dem_dense", "sweep", "drift"],
                    help="run only one extra section and print its JSON (for profiling)")
+    p.add_argument("--dem-steps", type=int, default=5000, help="steps of the DEM settling section")
     p.add_argument("--adjoint-steps", type=int, default=500)
     p.add_argument("--adjoint-every", type=int, default=50)
     p.add_argument("--adjoint-modes", default="native,fast", help="comma list of native, fast")
@@ -413,11 +414,15 @@ def bench_dem_settling(settle_steps=5000, sample_every=250):
     w = workloads.dem_settling(200000)
     s = ParticleSystem(w["config"], w["n"])
     workloads.load_into(s, w)
+    s.enable_graph(True)
     samples = []
+    graph_ms = []
     done = 0
     while done < settle_steps:
-        s.step(sample_every - 1)
-        s.timing_enable(True)
+        t0 = time.perf_counter()
+        s.step(sample_every - 1)  # graph-replayed, timed by the host clock (pg_step waits)
+        graph_ms.append(1e3 * (time.perf_counter() - t0) / (sample_every - 1))
+        s.timing_enable(True)  # the sampled step runs eagerly with stage events
         s.step_async(1)
         s.sync()
         t = s.timing_read()
@@ -430,6 +435,9 @@ def bench_dem_settling(settle_steps=5000, sample_every=250):
                             "kn 1e5, e 0.9, mu 0.3, dt 1e-6, f64, %d steps" % settle_steps,
                 "particles": w["n"], "steps": settle_steps, "timed": "one step in every %d" % sample_every,
                 "ms_per_step_median": settle_ms, "value": w["n"] / (settle_ms * 1e-3),
+                "graph_ms_per_step_median": statistics.median(graph_ms),
+                "graph_value": w["n"] / (statistics.median(graph_ms) * 1e-3),
+                "graph_timing": "host clock around %d graph-replayed steps between samples" % (sample_every - 1),
                 "contacts_max": max(x["contacts"] for x in samples),
                 "contacts_per_sample": [x["contacts"] for x in samples],
                 "note": "the spheres fall together (g t^2 / 2 = 0.12 mm in 5 ms), so pair contacts only start "
@@ -550,7 +558,8 @@ def run_gpu(args, rank, world, local, pgroup):
             if args.section == "adjoint":
                 res = bench_adjoint(args.adjoint_steps, args.adjoint_every, modes=args.adjoint_modes.split(","))
             else:
-                res = {"batched": bench_batched, "dem": bench_dem, "dem_dense": bench_dem_dense,
+                res = {"batched": bench_batched, "dem": lambda: bench_dem(settle_steps=args.dem_steps),
+                       "dem_settling": lambda: bench_dem_settling(args.dem_steps), "dem_dense": bench_dem_dense,
                        "sweep": bench_sweep, "drift": bench_drift}[args.section]()
             print(json.dumps({"section": args.section, args.section: res}), flush=True)
         return
