@@ -168,3 +168,24 @@ def test_batched_512_dam_breaks_bit_exact(pg, oracle):
         assert np.array_equal(rho[o:o + n], st.rho)
         o += n
     b.close()
+
+
+@pytest.mark.parametrize("mode,tol", [(0, 0.0), (1, 1e-4)])
+def test_lattice_4m_f32(pg, oracle, mode, tol):
+    """The 4M lattice in single precision: IEEE f32 bit-exact, contracted f32 within 1e-4, one step."""
+    w = workloads.sph_lattice_3d(n=4096000, seed=2, precision=0)
+    cfg = dict(w["config"], precision=0, f64_mode=mode)
+    s = ParticleSystem(make_config(**cfg), w["n"])
+    f = w["fields"]
+    for k in ("pos", "vel", "rho", "mass"):
+        s.set(k, np.asarray(f[k], np.float32))
+    st = oracle.SphState(np.asarray(f["pos"], np.float32), np.asarray(f["vel"], np.float32),
+                         np.asarray(f["rho"], np.float32), np.asarray(f["mass"], np.float32), f64=False)
+    s.step(1)
+    oracle.sph_run(cfg, st, 1)
+    if mode == 0:
+        assert np.array_equal(s.get("pos"), st.pos) and np.array_equal(s.get("rho"), st.rho)
+        assert np.array_equal(s.get("vel"), st.vel)
+    else:
+        assert _rel(s.get("pos"), st.pos) <= tol and _rel(s.get("rho"), st.rho) <= tol
+    s.close()
