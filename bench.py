@@ -291,7 +291,7 @@ def _peak_hbm():
     return 6800.0, "fallback"
 
 
-def bench_batched(steps=20, looped_steps=5, sync_steps=2):
+def bench_batched(steps=100, looped_steps=5, sync_steps=2):
     """512 independent 2D dam breaks: one batched handle (graph-replayed step) against looping
     the plain per-system handles over the same systems, (a) as the plain API is called, pg_step
     per system, and (b) enqueue-only with graph replay on 512 streams, synchronised once per
