@@ -1,6 +1,6 @@
 //! Raw bindings of the C ABI in include/prestige_gpu.h: one declaration per entry point, the
 //! structs with the header's field order and C layout.  The safe wrapper is in lib.rs.
-#![allow(non_camel_case_types)]
+#![allow(non_camel_case_types, non_snake_case)]
 
 use std::os::raw::{c_char, c_double, c_int, c_longlong, c_void};
 

@@ -124,7 +124,7 @@ pub struct System {
     raw: *mut ffi::pg_system,
     n: usize,
     dim: usize,
-    f64: bool,
+    double: bool,
     model: Model,
 }
 
@@ -161,7 +161,7 @@ impl System {
 
     fn wrap(raw: *mut ffi::pg_system, n: usize, c: &ffi::pg_config) -> System {
         let model = if c.model == ffi::PG_MODEL_DEM { Model::Dem } else { Model::Sph };
-        System { raw, n, dim: if model == Model::Dem { 3 } else { c.dim as usize }, f64: c.precision != ffi::PG_F32, model }
+        System { raw, n, dim: if model == Model::Dem { 3 } else { c.dim as usize }, double: c.precision != ffi::PG_F32, model }
     }
 
     pub fn len(&self) -> usize {
@@ -175,6 +175,10 @@ impl System {
     }
     pub fn model(&self) -> Model {
         self.model
+    }
+    /// True if the SPH state is stored in double precision (DEM state always is).
+    pub fn is_double(&self) -> bool {
+        self.double
     }
 
     /// Copy a named slice from the host (id order, vectors interleaved), in double precision;
