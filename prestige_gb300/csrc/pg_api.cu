@@ -223,8 +223,8 @@ int enqueue_neighbors(pg_system* s) {
 
 int mom_block(const pg_system* s) { return s->block_mom > 0 ? s->block_mom : s->block; }
 
-// Kernels enqueued by one neighbour search (hash, radix passes, cell count, scan).
-long long neighbor_launches(const pg_system* s) { return 1 + 3LL * s->nw.passes + 1 + (s->ncells ? 3 : 0); }
+// Kernels enqueued by one neighbour search (hash, radix passes, cell-start table).
+long long neighbor_launches(const pg_system* s) { return 1 + 3LL * s->nw.passes + 1; }
 
 // The continuity part of a step: neighbour search, sorted gather, neighbour lists and the
 // continuity pass (rho' into the canonical density and the sorted pack).  ev (optional): events

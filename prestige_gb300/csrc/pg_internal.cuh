@@ -105,9 +105,7 @@ struct NbrWork {
   DevBuf keys[2], vals[2];  // u32
   DevBuf hist;              // u32 [256 * tiles]
   DevBuf digit_total;       // u32 [256]
-  DevBuf cell_count;        // u32 [ncells]
   DevBuf cell_start;        // u32 [ncells + 1]
-  DevBuf scan_tmp;          // u32 block sums
   uint32_t* sorted_cell = nullptr;
   uint32_t* sorted_id = nullptr;
   int init(size_t n, uint64_t ncells);

@@ -225,10 +225,20 @@ __global__ void __launch_bounds__(kSortThreads) digit_scatter_kernel(
   }
 }
 
-// cell_count[c] = number of particles in cell c (integer atomics: the result is exact).
-__global__ void cell_count_kernel(const uint32_t* __restrict__ cell, size_t n, uint32_t* __restrict__ cnt) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) atomicAdd(&cnt[cell[i]], 1u);
+// cell_start[c] = first sorted slot whose cell is >= c, for c = 0 .. ncells (so cell_start[ncells]
+// = n), by a binary search over the sorted cells: one kernel, no count buffer and no scan.  The
+// threads of a warp search for consecutive cells, so they load the same midpoints on most steps.
+__global__ void cell_start_kernel(const uint32_t* __restrict__ cell, uint32_t n, uint32_t ncells,
+                                  uint32_t* __restrict__ start) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c > ncells) return;
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = lo + (hi - lo) / 2;
+    if (__ldg(cell + mid) < c) lo = mid + 1;
+    else hi = mid;
+  }
+  start[c] = lo;
 }
 
 int bits_needed(uint64_t v) {
@@ -273,15 +283,13 @@ int NbrWork::init(size_t n_, uint64_t ncells_) {
   PG_TRY(vals[1].ensure(nn * 4));
   PG_TRY(hist.ensure((size_t)kRadix * tiles * 4));
   PG_TRY(digit_total.ensure(kRadix * 4));
-  PG_TRY(cell_count.ensure((ncells ? ncells : 1) * 4));
   PG_TRY(cell_start.ensure((ncells + 1) * 4));
-  PG_TRY(scan_tmp.ensure(scan_tmp_words(ncells) * 4));
   return PG_OK;
 }
 
 size_t NbrWork::bytes() const {
   return keys[0].bytes + keys[1].bytes + vals[0].bytes + vals[1].bytes + hist.bytes + digit_total.bytes +
-         cell_count.bytes + cell_start.bytes + scan_tmp.bytes;
+         cell_start.bytes;
 }
 
 int sort_and_table(cudaStream_t st, NbrWork& w) {
@@ -308,11 +316,10 @@ int sort_and_table(cudaStream_t st, NbrWork& w) {
   }
   w.sorted_cell = w.keys[cur].as<uint32_t>();
   w.sorted_id = w.vals[cur].as<uint32_t>();
-  // cell table: count per cell, exclusive scan -> start (start[ncells] = n)
-  PG_CUDA_TRY(cudaMemsetAsync(w.cell_count.p, 0, w.ncells * 4, st));
-  if (n) cell_count_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(w.sorted_cell, n, w.cell_count.as<uint32_t>());
-  PG_TRY(launch_exclusive_scan(st, w.cell_count.as<uint32_t>(), w.cell_start.as<uint32_t>(), w.ncells,
-                               w.scan_tmp.as<uint32_t>()));
+  // cell table: start[c] = first slot of cell c (start[ncells] = n)
+  cell_start_kernel<<<(unsigned)((w.ncells + 1 + 255) / 256), 256, 0, st>>>(w.sorted_cell, (uint32_t)n,
+                                                                          (uint32_t)w.ncells,
+                                                                          w.cell_start.as<uint32_t>());
   PG_CUDA_TRY(cudaGetLastError());
   return PG_OK;
 }
