@@ -172,7 +172,8 @@ __device__ __forceinline__ void classify(const float4& pi, const float4& pj, flo
 
 // ---------------------------------------------------------------------------------------
 // Neighbour lists.  sph_list_kernel walks the candidates of every slot once per step and writes
-// the listed slots (classify: the FP32 superset, or with XD >= 0 exactly the f64 neighbours;
+// the listed slots (classify: with XD < 0 the FP32 test (exact for f32 systems), with XD >= 0
+// exactly the f64 neighbours;
 // never the slot itself) in walk order (rows z, then y ascending; slots ascending along a row)
 // to nlist in warp tiles (list_base: entry q of the 32 slots of a tile is one 128-byte line, so a
 // warp's reads of one entry index coalesce and its writes fill whole sectors while they are in

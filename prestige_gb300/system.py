@@ -196,8 +196,7 @@ class ParticleSystem:
 
     def pair_counts(self):
         """Lengths of the pair-pass neighbour lists built by the last step or compute_rates, per
-        sorted slot (exact neighbour counts, the particle itself excluded, in the f64
-        double-word mode; FP32 superset counts otherwise)."""
+        sorted slot (exact neighbour counts, the particle itself excluded)."""
         lengths = np.empty(self.n, np.uint32)
         nat.check(self._lib.pg_get_pair_lists(self._h, lengths.ctypes.data, None, 0), "pg_get_pair_lists")
         return lengths
