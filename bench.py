@@ -25,8 +25,8 @@ CPU arm is this project's restatement of the method in its CPU timing build (cel
 neighbour lists built once per step, OpenMP over all host threads).
 
 Multi-GPU (torchrun): every rank runs an independent replica of the workload on its own GPU
-(replicas only: the plain path is one spatial domain; see the design notes); value = all ranks'
-particle-steps / the slowest rank's time.
+(the 4M lattice fits one GPU, so the benchmark runs replicas; one system split across GPUs is
+prestige_gb300/slab.py); value = all ranks' particle-steps / the slowest rank's time.
 """
 import argparse
 import hashlib
