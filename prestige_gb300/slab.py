@@ -24,8 +24,9 @@ One step (SlabSPH.step):
   5. Migration: an owned particle whose new position lies in another slab moves to that rank (a
      step moves a particle by far less than a slab, so only to a neighbour).
 
-Each step creates the rank's handle for its current particle count (owned plus halo changes from
-step to step).  No CPU fallback: `make_handle` defaults to the GPU library.
+The rank's handle is kept while its local particle and fluid counts stay the same (every field
+is set anew each step) and is created again when they change.  No CPU fallback: `make_handle`
+defaults to the GPU library.
 """
 import numpy as np
 
@@ -84,6 +85,8 @@ class SlabSPH:
         self.vel = np.asarray(fields["vel"], np.float64)[mine].copy()
         self.rho = np.asarray(fields["rho"], np.float64)[mine].copy()
         self.mass = np.asarray(fields["mass"], np.float64)[mine].copy()
+        self._handle = None
+        self._handle_key = None
 
     # -- helpers -----------------------------------------------------------------------------
     def _owner(self, x):
@@ -126,8 +129,8 @@ class SlabSPH:
         where = np.empty_like(order)
         where[order] = np.arange(order.size)  # local index of each concatenated row
         n_local = gid.size
-        cfg = dict(self.cfg, n_fluid=int(np.count_nonzero(gid < self.n_fluid_global)))
-        h = self.make_handle(cfg, n_local)
+        n_fluid = int(np.count_nonzero(gid < self.n_fluid_global))
+        h = self._local_handle(n_local, n_fluid)
         try:
             h.set("pos", pos[order].reshape(n_local, d))
             h.set("vel", vel[order].reshape(n_local, d))
@@ -148,8 +151,9 @@ class SlabSPH:
             self.pos = np.asarray(h.get("pos"), np.float64).reshape(n_local, d)[own_local].copy()
             self.vel = np.asarray(h.get("vel"), np.float64).reshape(n_local, d)[own_local].copy()
             self.rho = np.asarray(h.get("rho"), np.float64)[own_local].copy()
-        finally:
-            h.close()
+        except BaseException:
+            self.close()
+            raise
         # 5. migration to the neighbour slabs
         dest = self._owner(self.pos[:, self.axis])
         if np.any(np.abs(dest - self.rank) > 1):
@@ -167,6 +171,22 @@ class SlabSPH:
         o = np.argsort(self.gid, kind="stable")
         self.gid, self.pos, self.vel, self.rho, self.mass = (self.gid[o], self.pos[o], self.vel[o], self.rho[o],
                                                              self.mass[o])
+
+    def _local_handle(self, n_local, n_fluid):
+        """The handle of the local system: the previous step's when the counts are the same (every
+        field is set anew each step), else a new one."""
+        if self._handle is not None and self._handle_key == (n_local, n_fluid):
+            return self._handle
+        self.close()
+        self._handle = self.make_handle(dict(self.cfg, n_fluid=n_fluid), n_local)
+        self._handle_key = (n_local, n_fluid)
+        return self._handle
+
+    def close(self):
+        if self._handle is not None:
+            self._handle.close()
+        self._handle = None
+        self._handle_key = None
 
     def run(self, nsteps):
         for _ in range(nsteps):

@@ -75,6 +75,7 @@ def _worker(rank, world, port, name, out):
     for _ in range(nsteps):
         slab.step()
         counts.append(int(slab.gid.size))
+    slab.close()
     pos, vel, rho = slab.gather()
     if rank == 0:
         with open(out, "wb") as f:

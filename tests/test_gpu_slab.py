@@ -110,6 +110,7 @@ def _rank(rank, world, port, mode, out):
     cfg = dict(w["config"], f64_mode=mode)
     slab = SlabSPH(cfg, w["fields"], dist, axis=0)
     slab.run(nsteps)
+    slab.close()
     pos, vel, rho = slab.gather()
     if rank == 0:
         with open(out, "wb") as f:
