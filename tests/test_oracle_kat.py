@@ -10,6 +10,9 @@ and the generated loop text), so the oracle is pinned here by answers derived by
   * SPH momentum: uniform motion gives a zero density rate exactly and, at uniform pressure,
     forces that cancel to rounding on the lattice interior; a linear density profile gives
     a = -grad(p)/rho to < 1.5 % and no transverse force;
+  * SPH pair forces: on a disordered cloud with viscosity, unequal masses and densities, total
+    linear and angular momentum rates vanish to rounding (antisymmetric, central pair terms),
+    and rotating the configuration rotates the accelerations (isotropy);
   * DEM: a head-on collision rebounds with the restitution coefficient, and a sphere resting
     on the floor settles at the overlap m g / kn;
   * the dual-number gradient equals central finite differences of the double run.
@@ -187,3 +190,54 @@ def test_oracle_states_do_not_alias_inputs(oracle):
     oracle.sph_run(w["config"], st, 2)
     for k in f:
         assert np.array_equal(f[k], w["fields"][k])
+
+
+def _random_cloud(dim, n=1500, seed=3, dx=0.01):
+    """A disordered cloud (a jittered lattice, random velocities and densities) in free space."""
+    rng = np.random.default_rng(seed)
+    side = int(round(n ** (1.0 / dim)))
+    pos = lattice(side, dim, dx) + rng.uniform(-0.3 * dx, 0.3 * dx, size=(side ** dim, dim))
+    m = pos.shape[0]
+    vel = rng.normal(0.0, 0.5, size=pos.shape)
+    rho = 1000.0 * (1.0 + rng.uniform(-0.02, 0.02, size=m))
+    mass = 1000.0 * dx ** dim * (1.0 + rng.uniform(-0.1, 0.1, size=m))
+    return pos, vel, rho, mass
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_pair_forces_conserve_momentum(oracle, dim):
+    """Every pair term is antisymmetric (the symmetric factor (P_i + P_j + Pi_ij) F_ij times
+    x_ij = -x_ji, weighted by the partner's mass), so sum_i m_i a_i vanishes to rounding, with
+    viscosity on and unequal masses and densities."""
+    dx = 0.01
+    pos, vel, rho, mass = _random_cloud(dim, dx=dx)
+    cfg = sph_cfg(dim, 1.3 * dx, alpha=0.3)
+    acc, _ = oracle.sph_rates(cfg, oracle.SphState(pos, vel, rho, mass))
+    total = (mass[:, None] * acc).sum(axis=0)
+    scale = np.abs(mass[:, None] * acc).sum(axis=0)
+    assert np.all(np.abs(total) <= 1e-12 * scale)
+
+
+def test_pair_forces_conserve_angular_momentum(oracle):
+    """The pair forces act along x_ij, so sum_i m_i x_i x a_i vanishes to rounding (3D)."""
+    dx = 0.01
+    pos, vel, rho, mass = _random_cloud(3, dx=dx)
+    acc, _ = oracle.sph_rates(sph_cfg(3, 1.3 * dx, alpha=0.3), oracle.SphState(pos, vel, rho, mass))
+    torque = np.cross(pos, mass[:, None] * acc)
+    assert np.all(np.abs(torque.sum(axis=0)) <= 1e-12 * np.abs(torque).sum(axis=0))
+
+
+def test_rates_rotate_with_the_configuration(oracle):
+    """Rotating positions and velocities rotates the accelerations and leaves the density rates
+    unchanged (the method has no preferred direction; the cell grid only orders the sums)."""
+    dx = 0.01
+    pos, vel, rho, mass = _random_cloud(3, n=1200, dx=dx)
+    cfg = sph_cfg(3, 1.3 * dx, alpha=0.3)
+    a0, d0 = oracle.sph_rates(cfg, oracle.SphState(pos, vel, rho, mass))
+    q, _ = np.linalg.qr(np.random.default_rng(8).normal(size=(3, 3)))
+    centre = pos.mean(axis=0)
+    pos_r = (pos - centre) @ q.T + 0.25
+    a1, d1 = oracle.sph_rates(cfg, oracle.SphState(pos_r, vel @ q.T, rho, mass))
+    scale = np.abs(a0).max()
+    assert np.abs(a1 - a0 @ q.T).max() <= 1e-9 * scale
+    assert np.abs(d1 - d0).max() <= 1e-9 * np.abs(d0).max()
