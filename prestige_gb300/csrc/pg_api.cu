@@ -1316,6 +1316,7 @@ int pg_step_stage(pg_system* s, int stage) {
   s->stage_pending = false;
   SphArgs a = pg::sph_args(s, 1, false);
   PG_TRY(pg::launch_sph_repack_rho(s->stream, a, s->arith));
+  s->launches += 1;
   PG_TRY(pg::enqueue_sph_momentum(s, nullptr));
   return pg::sync_and_check(s);
 }
