@@ -88,3 +88,24 @@ def test_dem_contact_overflow_reported(pg, oracle):
     assert c == -1
     assert np.array_equal(s.get("pos"), st.pos)
     assert np.array_equal(s.get("vel"), st.vel)
+
+
+@pytest.mark.parametrize("overlap", [0.4, 0.5])
+def test_dem_more_contacts_than_the_walk_buffer(pg, oracle, overlap):
+    """Lattices so compressed that many spheres have 17 to 29 contacts (walls included): the
+    walk's per-thread contact buffer (16 entries) fills, the lane evaluates the first contacts
+    itself before walking on, and the warp evaluates the rest; bit-exact with the oracle."""
+    w = compressed_lattice(nside=(6, 6, 6), overlap=overlap, capacity=32)
+    s = _run_pair(w, 0, 0)
+    st = _ostate(oracle, w)
+    for _ in range(2):
+        s.step(1)
+        c, _ = oracle.dem_run(w["config"], st, 1)
+        assert s.dem_contacts() == c
+        assert np.array_equal(s.get("pos"), st.pos)
+        assert np.array_equal(s.get("vel"), st.vel)
+        assert np.array_equal(s.get("omega"), st.omega)
+        pid, xi = s.dem_history()
+        assert np.array_equal(pid.reshape(-1), st.hpid)
+        assert np.array_equal(xi.reshape(-1), st.hxi)
+    assert ((pid != 0xFFFFFFFF).sum(axis=1) > 16).any()
