@@ -76,6 +76,15 @@ def test_eq1_source_is_the_plain_gather():
     assert "pg_p_force[id] = pg_force_i;" in src
 
 
+def test_token_stream_text_translates_like_the_compact_form():
+    """fuse() keeps each body as TokenStream text (prestige/src/equations/fuse.rs:34), which
+    spaces every token: `force [i] += mass [j] ;`.  It gives the same CUDA source."""
+    st1, compact = _source(["force[i] += mass[j]"])
+    st2, spaced = _source(["force [i] += mass [j] ;"])
+    assert st1 == st2 == _native.PG_OK
+    assert spaced == compact
+
+
 # ------------------------------------------------------------------------------------------
 def _system(w, **over):
     s = ParticleSystem(make_config(**dict(w["config"], **over)), w["n"])
