@@ -77,7 +77,7 @@ def test_eq1_source_is_the_plain_gather():
 
 
 def test_token_stream_text_translates_like_the_compact_form():
-    """fuse() keeps each body as TokenStream text (prestige/src/equations/fuse.rs:34), which
+    """fuse() keeps each body as TokenStream text (prestige/src/equations/fuse.rs:30), which
     spaces every token: `force [i] += mass [j] ;`.  It gives the same CUDA source."""
     st1, compact = _source(["force[i] += mass[j]"])
     st2, spaced = _source(["force [i] += mass [j] ;"])
