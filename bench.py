@@ -12,11 +12,12 @@ resident in HBM (CUDA events on the library's stream, max over ranks); `e2e` = t
 through the public C ABI with host buffers (pinned) copied in and out every step, pipelined
 with the asynchronous field calls so the copies overlap the neighbouring steps.  `roofline`
 describes the momentum pass, the step's longest kernel launch (the continuity pass, of about
-the same total time, runs as two launches beside the neighbour lists).  Unless --no-extras, five more
+the same total time, runs as two launches beside the neighbour lists).  Unless --no-extras, six more
 sections on rank 0: `batched` (512 uneven 2D dam breaks in one handle vs looping the plain
 handles), `adjoint` (backward / forward cost of the differentiable 3D workload), `dem`
 (200,000 spheres: the settling run over its 5,000 steps, and a contact-dense compressed lattice),
-`drift` (the double-word trajectory against the IEEE one over whole runs) and `sweep` (the
+`dam_break` (the 2D dam break at dx = 0.02 over its 2,000 steps), `drift` (the double-word
+trajectory against the IEEE one over whole runs) and `sweep` (the
 lattice at 256k, 1M and 4M particles in f64 and f32, double-word / fast and IEEE arithmetic).
 
 `--impl reference` times the CPU path on the host cores instead: the reference has no executable
@@ -91,7 +92,8 @@ def parse():
     p.add_argument("--mom-block", type=int, default=0, help="momentum-pass block size used with --block (0: --block)")
     p.add_argument("--ppw", type=int, default=32, help="particles per warp of the pair passes used with --block")
     p.add_argument("--section", default="all",
-                   choices=["all", "batched", "adjoint", "dem", "dem_settling", "dem_dense", "sweep", "drift"],
+                   choices=["all", "batched", "adjoint", "dem", "dem_settling", "dem_dense", "dam_break", "sweep",
+                            "drift"],
                    help="run only one extra section and print its JSON (for profiling)")
     p.add_argument("--dem-steps", type=int, default=5000, help="steps of the DEM settling section")
     p.add_argument("--adjoint-steps", type=int, default=500)
@@ -481,6 +483,33 @@ def bench_dem_dense(dense_steps=20, dense_warmup=3):
     return dense
 
 
+def bench_dam(steps=2000):
+    """The 2D dam break at dx = 0.02 (5,000 fluid + 1,518 wall particles), its 2,000 steps,
+    graph-replayed, in both f64 modes: a small system, bound by launch latency rather than by
+    any pipe (host clock around the run, stream synchronised)."""
+    import torch
+
+    from prestige_gb300 import ParticleSystem, make_config, workloads
+    w = workloads.dam_break_2d(dx=0.02)
+    out = {"workload": "2D dam break, dx = 0.02, 5,000 fluid + 1,518 wall particles, %d steps" % steps,
+           "particles": w["n"], "steps": steps, "unit": "particle-steps/s",
+           "timing": "host clock around the graph-replayed run"}
+    for mode, name in ((1, "double_word"), (0, "ieee")):
+        s = ParticleSystem(make_config(**dict(w["config"], f64_mode=mode)), w["n"])
+        workloads.load_into(s, w)
+        s.enable_graph(True)
+        s.step(3)
+        workloads.load_into(s, w)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.step(steps)
+        sec = time.perf_counter() - t0
+        front = float(s.get("pos")[:w["n_fluid"], 0].max())
+        s.close()
+        out[name] = {"ms_per_step": 1e3 * sec / steps, "value": w["n"] * steps / sec, "front_x_m": front}
+    return out
+
+
 def bench_drift(n=4096000, lattice_steps=100, lattice_every=10, dam_steps=2000, dam_every=100):
     """Trajectory drift of the double-word f64 mode: its trajectory against the IEEE f64 one (which
     reproduces the oracle bit for bit), without resetting the state, on the 4M lattice for 100
@@ -566,7 +595,7 @@ def run_gpu(args, rank, world, local, pgroup):
             else:
                 res = {"batched": bench_batched, "dem": lambda: bench_dem(settle_steps=args.dem_steps),
                        "dem_settling": lambda: bench_dem_settling(args.dem_steps), "dem_dense": bench_dem_dense,
-                       "sweep": bench_sweep, "drift": bench_drift}[args.section]()
+                       "dam_break": bench_dam, "sweep": bench_sweep, "drift": bench_drift}[args.section]()
             print(json.dumps({"section": args.section, args.section: res}), flush=True)
         return
     w = workload(args)
@@ -724,6 +753,7 @@ def run_gpu(args, rank, world, local, pgroup):
             out["adjoint"] = bench_adjoint(args.adjoint_steps, args.adjoint_every,
                                            modes=args.adjoint_modes.split(","))
             out["dem"] = bench_dem()
+            out["dam_break"] = bench_dam()
             out["drift"] = bench_drift(n)
             out["sweep"] = bench_sweep()
         print(json.dumps(out), flush=True)
