@@ -27,7 +27,10 @@ neighbour lists built once per step, OpenMP over all host threads).
 
 Multi-GPU (torchrun): every rank runs an independent replica of the workload on its own GPU
 (the 4M lattice fits one GPU, so the benchmark runs replicas; one system split across GPUs is
-prestige_gb300/slab.py); value = all ranks' particle-steps / the slowest rank's time.
+prestige_gb300/slab.py); value = all ranks' particle-steps / the slowest rank's time.  Unless
+--no-extras, the line then also carries `batched_sharded`: the 512 dam breaks bin-packed over the
+ranks by particle count (prestige_gb300/batch_shard.py, one batched handle per rank, nothing
+exchanged while they step), all systems' particle-steps over the slowest rank's time.
 """
 import argparse
 import hashlib
@@ -374,6 +377,39 @@ def bench_batched(steps=100, looped_steps=5, sync_steps=2):
                       "steps with CUDA events"}
 
 
+def bench_batched_sharded(rank, world, pgroup, steps=100):
+    """The 512 dam breaks of `bench_batched` bin-packed over the ranks by particle count, one
+    batched handle (graph-replayed step) per rank and no collective while they step: all systems'
+    particle-steps over the slowest rank's time (the total work is fixed: strong scaling)."""
+    import torch
+
+    from prestige_gb300 import workloads
+    from prestige_gb300.batch_shard import ShardedBatch
+    systems = workloads.batched_dam_breaks()
+    for w in systems:
+        w["config"] = dict(w["config"], f64_mode=1)
+    sb = ShardedBatch(systems, rank, world)
+    try:
+        sb.enable_graph(True)
+        sb.step(3)
+        torch.cuda.synchronize()
+        barrier(pgroup)
+        t0 = time.perf_counter()
+        sb.step(steps)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        barrier(pgroup)
+    finally:
+        sb.close()
+    tmax = allmax(pgroup, t)
+    loads = sb.particles_per_rank()
+    return {"workload": "the batched section's 512 dam breaks, f64 double-word mode", "ranks": world,
+            "systems_per_rank": [len(x) for x in sb.packing], "particles_per_rank": loads,
+            "unit": "particle-steps/s", "value": sum(loads) * steps / tmax, "ms_per_step": 1e3 * tmax / steps,
+            "steps": steps, "scaling": "strong",
+            "timing": "host wall clock around graph-replayed steps, stream synchronised, max over ranks"}
+
+
 def bench_adjoint(nsteps=500, every=50, n=100000, modes=("native", "fast")):
     """Differentiable 3D SPH: forward with checkpoints, then the adjoint sweep (recompute +
     adjoint passes); cost of a backward step over a forward step."""
@@ -681,6 +717,7 @@ def run_gpu(args, rank, world, local, pgroup):
     e2e_s = allmax(pgroup, e2e_s)
     e2e_value = world * n * args.e2e_steps / e2e_s
     s.close()
+    sharded = bench_batched_sharded(rank, world, pgroup) if world > 1 and not args.no_extras else None
 
     if rank == 0:
         cpu = None
@@ -748,6 +785,8 @@ def run_gpu(args, rank, world, local, pgroup):
                      "arith": info["arith"], "overlap_split": info.get("overlap_split", 0)},
             "tuning": tuning,
         }
+        if sharded is not None:
+            out["batched_sharded"] = sharded
         if not args.no_extras:
             out["batched"] = bench_batched()
             out["adjoint"] = bench_adjoint(args.adjoint_steps, args.adjoint_every,

@@ -86,6 +86,7 @@ SphK make_sphk(const pg_config& c, const Grid& g, uint32_t cell_base, uint32_t i
   k.w.h = (float)h;
   k.w.band = (float)(1e-9 * k.d.four_h2);
   k.two_h_f = (float)(2.0 * h) * 1.0000001f;
+  k.pos_pad = 8.0 * h;
   k.id_begin = id_begin;
   k.id_end = id_end;
   k.fluid_end = fluid_end;
@@ -149,10 +150,7 @@ int ensure_sorted_buffers(pg_system* s) {
     PG_TRY(s->fcache.ensure(16 * ((n + kListTile - 1) / kListTile) * kListTile * (size_t)s->list_cap));
   PG_TRY(s->nlen.ensure(4 * n));
   PG_TRY(s->nresume.ensure(8 * n));
-  PG_TRY(s->posmin.ensure(3 * sizeof(unsigned long long)));
-  double hmax = 0.0;
-  for (const pg_config& c : s->cfgs) hmax = std::max(hmax, c.h);
-  s->pos_pad = 8.0 * hmax;
+  PG_TRY(s->posmin.ensure(3 * sizeof(unsigned long long) * (size_t)s->nsys));
   return PG_OK;
 }
 
@@ -183,7 +181,6 @@ SphArgs sph_args(pg_system* s, int integrate, bool rates) {
   a.cap = (uint32_t)s->list_cap;
   a.err = s->err.as<unsigned>();
   a.posmin = s->posmin.as<unsigned long long>();
-  a.pos_pad = s->pos_pad;
   a.k_begin = 0;
   a.k_end = (uint32_t)s->n;
   return a;
@@ -209,11 +206,11 @@ NbrArgs nbr_args(pg_system* s) {
 int enqueue_neighbors(pg_system* s) {
   s->stage_pending = false;  // any neighbour search ends a pending pg_step_stage(0)
   const void* pos = s->pos.p;
-  // the double-word packs need the step's minimum position (sph_gather_df)
+  // the double-word packs need each system's minimum position of the step (sph_gather_df)
   unsigned long long* posmin = nullptr;
   if (s->model == PG_MODEL_SPH && s->arith == ARITH_F64_DF && s->posmin.p) {
     posmin = s->posmin.as<unsigned long long>();
-    PG_CUDA_TRY(cudaMemsetAsync(posmin, 0xff, 3 * sizeof(unsigned long long), s->stream));
+    PG_CUDA_TRY(cudaMemsetAsync(posmin, 0xff, 3 * sizeof(unsigned long long) * (size_t)s->nsys, s->stream));
   }
   PG_TRY(launch_hash(s->stream, s->gridk.as<GridK>(), s->nsys > 1 ? s->sys_of_id.as<uint32_t>() : nullptr, s->f64,
                      s->dim, pos, s->n, s->nw.keys[0].as<uint32_t>(), s->nw.vals[0].as<uint32_t>(), posmin));

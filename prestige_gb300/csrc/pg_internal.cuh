@@ -113,8 +113,8 @@ struct NbrWork {
 };
 
 // Cell key and id of every particle (id order) into w.keys[0] / w.vals[0].
-// posmin (optional, f64 positions only): per-dimension minimum position, as ordered_code values,
-// folded in with atomicMin (the caller presets it to all ones).
+// posmin (optional, f64 positions only): per system and dimension ([3 sys + d]) the minimum
+// position, as ordered_code values, folded in with atomicMin (the caller presets it to all ones).
 int launch_hash(cudaStream_t st, const GridK* grid_dev, const uint32_t* sys_of_id, int f64, int dim,
                 const void* pos, size_t n, uint32_t* keys, uint32_t* vals, unsigned long long* posmin = nullptr);
 

@@ -53,6 +53,7 @@ struct SphK {
   SphC<float> f;
   SphDF w;
   float two_h_f;
+  double pos_pad;                        // double-word mode: 8h, packed positions are x - min + pos_pad
   double avk_alpha;                      // d avk / d alpha = -2 c0 h (adjoint)
   uint32_t id_begin, id_end, fluid_end;  // global ids; ids >= fluid_end are fixed wall particles
   int gamma;
@@ -73,9 +74,8 @@ struct SphArgs {
   void* mass;
   void* acc;                 // optional rates output, id order
   void* drho;
-  unsigned long long* posmin;  // double-word mode: per-dimension minimum position of the step,
-                               // order-preserving integer code (pos_min_kernel)
-  double pos_pad;              // double-word mode: packed positions are x - min + pos_pad (>= 8h)
+  unsigned long long* posmin;  // double-word mode: per system and dimension ([3 sys + d]) the minimum
+                               // position of the step, order-preserving integer code (hash_kernel)
   void* lam[5];              // adjoint (pg_adjoint.cu): lambda_x, lambda_v, lambda_rho, dL/dalpha and
                              // dL/dB partial sums, all id order
   uint32_t* nlist;           // neighbour lists in tiles of kListTile slots: entry q of slot k at

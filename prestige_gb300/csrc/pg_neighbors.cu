@@ -156,8 +156,11 @@ __device__ __forceinline__ int cell_coord_f(float x, float lo, float inv, int n)
   return (int)t;
 }
 
-// Cell key and id of every particle.  MIN: also the per-dimension minimum position (block
-// reduction, one atomicMin per block and dimension; blockDim.x == 256).
+// Cell key and id of every particle.  MIN: also the minimum position per system and dimension
+// (posmin[3 sys + d]).  A single system: block reduction, one atomicMin per block and dimension
+// (blockDim.x == 256).  A batch: warp reduction where the warp's particles belong to one system
+// (ids are contiguous per system, so all warps but those at a system boundary), else one
+// atomicMin per particle.
 template <class R, int DIM, bool MIN>
 __global__ void hash_kernel(const GridK* __restrict__ grid, const uint32_t* __restrict__ sys_of_id,
                             const R* __restrict__ pos, uint32_t n, uint32_t* __restrict__ keys,
@@ -178,7 +181,20 @@ __global__ void hash_kernel(const GridK* __restrict__ grid, const uint32_t* __re
     keys[i] = g.cell_base + ((uint32_t)c[2] * (uint32_t)g.ny + (uint32_t)c[1]) * (uint32_t)g.nx + (uint32_t)c[0];
     vals[i] = i;
   }
-  if (MIN) {
+  if (MIN && sys_of_id) {
+    const uint32_t s = i < n ? sys_of_id[i] : 0xffffffffu;
+    const uint32_t s0 = __shfl_sync(0xffffffffu, s, 0);
+    if (__all_sync(0xffffffffu, s == s0)) {
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        for (int o = 16; o; o >>= 1) m[d] = min(m[d], __shfl_down_sync(0xffffffffu, m[d], o));
+        if ((threadIdx.x & 31) == 0 && s0 != 0xffffffffu) atomicMin(posmin + 3 * (size_t)s0 + d, m[d]);
+      }
+    } else if (i < n) {
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) atomicMin(posmin + 3 * (size_t)s + d, m[d]);
+    }
+  } else if (MIN) {
     __shared__ unsigned long long part[DIM][8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll

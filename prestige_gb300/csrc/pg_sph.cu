@@ -133,17 +133,19 @@ struct __align__(64) DfRecord {
 };
 
 // Packs of the double-word mode.  Positions in the record and in the FP32 array are shifted by
-// pos_pad - min (per dimension), so every packed coordinate is at least 8h: the hi parts of two
-// particles closer than 2h are then within a factor 2 of each other and the pair passes take
-// differences with df_sub_close.  The shift is common to all particles, so differences are
-// unchanged up to one f64 rounding of each shifted coordinate; the f64 array for the exact test
-// keeps the unshifted positions.
+// pos_pad - min (per system and dimension, pos_pad = 8h of the system), so every packed coordinate
+// is at least 8h: the hi parts of two particles closer than 2h are then within a factor 2 of each
+// other and the pair passes take differences with df_sub_close.  The shift is common to all
+// particles of a system (pairs never cross systems), so differences are unchanged up to one f64
+// rounding of each shifted coordinate, and a system's packs, hence its results, do not depend on
+// the other systems of a batch; the f64 array for the exact test keeps the unshifted positions.
 template <int DIM>
 __global__ void sph_gather_df(SphArgs a) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= a.n) return;
   const uint32_t id = a.sorted_id[k];
-  const SphK& K = a.sys[sys_of_slot(a, id)];
+  const uint32_t sys = sys_of_slot(a, id);
+  const SphK& K = a.sys[sys];
   const double* pos = (const double*)a.pos;
   const double* vel = (const double*)a.vel;
   const double rho = ((const double*)a.rho)[id];
@@ -154,9 +156,9 @@ __global__ void sph_gather_df(SphArgs a) {
     x[c] = pos[(size_t)id * DIM + c];
     v[c] = vel[(size_t)id * DIM + c];
   }
-  double xs[3] = {a.pos_pad, a.pos_pad, a.pos_pad};
+  double xs[3] = {K.pos_pad, K.pos_pad, K.pos_pad};
 #pragma unroll
-  for (int c = 0; c < DIM; ++c) xs[c] = __dadd_rn(__dsub_rn(x[c], ordered_value(a.posmin[c])), a.pos_pad);
+  for (int c = 0; c < DIM; ++c) xs[c] = __dadd_rn(__dsub_rn(x[c], ordered_value(a.posmin[3 * sys + c])), K.pos_pad);
   float4 ah, al, bh, bl;
   df_split_fast(xs[0], &ah.x, &al.x);
   df_split_fast(xs[1], &ah.y, &al.y);

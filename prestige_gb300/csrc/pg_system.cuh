@@ -63,7 +63,6 @@ struct pg_system {
   pg::DevBuf nlist, nlen, nresume;
   pg::DevBuf fcache;             // double-word mode: F per list entry (continuity -> momentum)
   pg::DevBuf posmin;             // 3 x u64, double-word mode (pos_min_kernel)
-  double pos_pad = 0.0;          // 8 x the largest h of the handle's systems
 
   // DEM contact history, id order, double buffered
   pg::DevBuf hpid[2], hxi[2];

@@ -110,3 +110,24 @@ def test_batch_overlapped_step_within_tolerance(pg, oracle):
         assert np.abs(rho[o:o + n] - st.rho).max() <= F64_TOL * np.abs(st.rho).max()
         o += n
     b.close()
+
+
+def test_double_word_system_alone_equals_it_in_a_batch(pg):
+    """The double-word packs are shifted per system, so a system's bits do not depend on the
+    other systems of its batch: each system stepped alone equals it stepped in the batch."""
+    systems = _small_systems(count=5, seed=9)
+    b = _batch(systems, 1)
+    b.step(4)
+    pos, vel, rho = b.get("pos"), b.get("vel"), b.get("rho")
+    b.close()
+    o = 0
+    for w in systems:
+        n = w["n"]
+        s = ParticleSystem(dict(w["config"], f64_mode=1), n)
+        workloads.load_into(s, w)
+        s.step(4)
+        assert np.array_equal(s.get("pos"), pos[o:o + n])
+        assert np.array_equal(s.get("vel"), vel[o:o + n])
+        assert np.array_equal(s.get("rho"), rho[o:o + n])
+        s.close()
+        o += n
