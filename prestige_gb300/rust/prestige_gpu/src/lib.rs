@@ -311,6 +311,24 @@ impl System {
         Ok(c)
     }
 
+    /// DEM: the tangential history, id order: partner ids (n * capacity; 0xFFFFFFF0 + face for
+    /// a wall, u32::MAX for an empty slot) and springs (n * capacity * 3).  `capacity` is the
+    /// configuration's contact capacity (the library refuses any other).
+    pub fn dem_history(&mut self, capacity: usize) -> Result<(Vec<u32>, Vec<f64>)> {
+        let mut partner = vec![0u32; self.n * capacity];
+        let mut xi = vec![0.0f64; self.n * capacity * 3];
+        check(unsafe { ffi::pg_dem_get_history(self.raw, partner.as_mut_ptr(), xi.as_mut_ptr(), capacity) })?;
+        Ok((partner, xi))
+    }
+
+    /// DEM: replace the tangential history (the layout of `dem_history`).
+    pub fn set_dem_history(&mut self, partner: &[u32], xi: &[f64], capacity: usize) -> Result<()> {
+        if partner.len() != self.n * capacity || xi.len() != self.n * capacity * 3 {
+            return Err(Error { status: ffi::PG_EINVAL, message: "history of n * capacity partners and springs".into() });
+        }
+        check(unsafe { ffi::pg_dem_set_history(self.raw, partner.as_ptr(), xi.as_ptr(), capacity) })
+    }
+
     /// Differentiable run: nsteps from the current state, checkpoints every `every` steps.
     pub fn forward_checkpointed(&mut self, nsteps: i32, every: i32) -> Result<()> {
         check(unsafe { ffi::pg_forward_checkpointed(self.raw, nsteps, every) })

@@ -1,4 +1,4 @@
-"""One SPH system split into slabs across ranks (one GPU each), with a halo exchange per step.
+"""One SPH or DEM system split into slabs across ranks (one GPU each), with a halo exchange per step.
 
 The reference runs its pairwise loop over one set of slices (prestige/src/codegen/simple_cpu.rs:
 7-19); a system too large for one GPU is split here along one axis into slabs, one per rank, and
@@ -27,6 +27,9 @@ One step (SlabSPH.step):
 The rank's handle is kept while its local particle and fluid counts stay the same (every field
 is set anew each step) and is created again when they change.  No CPU fallback: `make_handle`
 defaults to the GPU library.
+
+SlabDEM (below) is the same decomposition for a DEM system: a band of 2 r_max, one stage per
+step, and the tangential contact history carried in global ids.
 """
 import numpy as np
 
@@ -201,3 +204,193 @@ class SlabSPH:
         assert np.array_equal(gid[o], np.arange(self.n_global))
         return (np.concatenate([p[1] for p in parts])[o], np.concatenate([p[2] for p in parts])[o],
                 np.concatenate([p[3] for p in parts])[o])
+
+
+# ------------------------------------------------------------------------------------------------
+# DEM slabs
+# ------------------------------------------------------------------------------------------------
+WALL_ID = 0xFFFFFFF0  # partner codes WALL_ID + face in the contact history
+NO_PARTNER = 0xFFFFFFFF  # an empty history slot (the slots after a particle's last contact)
+
+
+class SlabDEM:
+    """This rank's slab of one DEM system (pg_step: the contact pass with its integrator).
+
+    The same cuts, ownership and migration as SlabSPH, along `axis` (the longest, z, by default).
+    One step is one stage: a sphere's force and torque depend on the positions, velocities and
+    spins of the spheres in contact with it and on its own tangential history, so
+      1. each rank sends each neighbour its owned spheres within 2 r_max of the shared cut (any
+         contact partner of an owned sphere, at a distance below r_i + r_j <= 2 r_max, is owned or
+         in that band on the other side);
+      2. the local system is the owned and halo spheres in global-id order on the global cell
+         grid and walls, so the contact walk meets the spheres of a cell in the single-domain order;
+      3. the owned spheres' tangential history (partner global ids, walls as WALL_ID + face) is
+         translated to local ids and set; halo spheres start empty (their results are dropped);
+         a partner absent from the local system cannot be in contact, so its entry is dropped (the
+         history holds the contacts of the last step, in the order found);
+      4. one step; the owned spheres keep the result and their history, translated back to
+         global ids;
+      5. spheres that crossed a cut migrate, with their history.
+
+    fields: the whole system's "pos", "vel", "omega", "radius", "mass" in global-id order, plus
+    optionally "history": (partner ids (n, C), springs (n, C, 3)) in global ids."""
+
+    def __init__(self, cfg, fields, dist, axis=2, make_handle=gpu_handle):
+        self.cfg = dict(cfg)
+        self.dist = dist
+        self.rank = dist.get_rank()
+        self.world = dist.get_world_size()
+        self.axis = axis
+        self.make_handle = make_handle
+        pos = np.asarray(fields["pos"], np.float64)
+        self.n_global = pos.shape[0]
+        self.C = int(self.cfg.get("contact_capacity", 16))
+        self.halo = 2.0 * float(self.cfg["r_max"])
+        q = np.quantile(pos[:, axis], [r / self.world for r in range(1, self.world)]) if self.world > 1 else []
+        self.cuts = np.concatenate([[-np.inf], np.asarray(q, np.float64), [np.inf]])
+        mine = self._owner(pos[:, axis]) == self.rank
+        self.gid = np.nonzero(mine)[0].astype(np.int64)
+        self.f = {k: np.asarray(fields[k], np.float64)[mine].copy() for k in ("pos", "vel", "omega", "radius", "mass")}
+        if "history" in fields:
+            hp, hx = fields["history"]
+            self.hpid = np.asarray(hp, np.uint32).reshape(self.n_global, self.C)[mine].copy()
+            self.hxi = np.asarray(hx, np.float64).reshape(self.n_global, self.C, 3)[mine].copy()
+        else:
+            self.hpid = np.full((self.gid.size, self.C), NO_PARTNER, np.uint32)
+            self.hxi = np.zeros((self.gid.size, self.C, 3))
+        self._handle = None
+        self._handle_n = None
+
+    def _owner(self, x):
+        return np.searchsorted(self.cuts, x, side="right") - 1
+
+    def _neighbours(self):
+        x = self.f["pos"][:, self.axis]
+        out = []
+        if self.rank > 0:
+            out.append((self.rank - 1, x < self.cuts[self.rank] + self.halo))
+        if self.rank < self.world - 1:
+            out.append((self.rank + 1, x >= self.cuts[self.rank + 1] - self.halo))
+        return out
+
+    # rows: gid, pos (3), vel (3), omega (3), radius, mass [, partner ids (C), springs (3C)]
+    def _rows(self, sel, history):
+        cols = [self.gid[sel, None].astype(np.float64), self.f["pos"][sel], self.f["vel"][sel], self.f["omega"][sel],
+                self.f["radius"][sel, None], self.f["mass"][sel, None]]
+        if history:
+            cols += [self.hpid[sel].astype(np.float64), self.hxi[sel].reshape(-1, 3 * self.C)]
+        return np.concatenate(cols, axis=1)
+
+    def _unpack(self, rows, history):
+        out = {"gid": rows[:, 0].astype(np.int64), "pos": rows[:, 1:4], "vel": rows[:, 4:7], "omega": rows[:, 7:10],
+               "radius": rows[:, 10], "mass": rows[:, 11]}
+        if history:
+            C = self.C
+            out["hpid"] = rows[:, 12:12 + C].astype(np.uint32)
+            out["hxi"] = rows[:, 12 + C:12 + 4 * C].reshape(-1, C, 3)
+        return out
+
+    @staticmethod
+    def _compact(hp, hx, keep):
+        """Keep the marked entries of each row in order, the rest of the row empty."""
+        out_p = np.full_like(hp, NO_PARTNER)
+        out_x = np.zeros_like(hx)
+        r, c = np.nonzero(keep)
+        dst = (np.cumsum(keep, axis=1) - 1)[r, c]
+        out_p[r, dst] = hp[r, c]
+        out_x[r, dst] = hx[r, c]
+        return out_p, out_x
+
+    def _history_to_local(self, g2l):
+        hp = self.hpid.astype(np.int64)
+        live = np.cumprod(hp != NO_PARTNER, axis=1).astype(bool)  # up to the first empty slot
+        particle = live & (hp < WALL_ID)
+        mapped = np.where(particle, g2l[np.where(particle, hp, 0)], hp)
+        keep = live & ((hp >= WALL_ID) | (mapped >= 0))
+        return self._compact(mapped.astype(np.uint32), self.hxi, keep)
+
+    @staticmethod
+    def _history_to_global(hp, gid_local):
+        hp = np.asarray(hp, np.int64)
+        particle = hp < WALL_ID
+        return np.where(particle, gid_local[np.where(particle, hp, 0)], hp).astype(np.uint32)
+
+    def step(self):
+        peers = self._neighbours()
+        halo = [self._unpack(_exchange(self.dist, peer, self._rows(sel, False)), False) for peer, sel in peers]
+        gid = np.concatenate([self.gid] + [h["gid"] for h in halo])
+        order = np.argsort(gid, kind="stable")
+        where = np.empty_like(order)
+        where[order] = np.arange(order.size)
+        n_local = gid.size
+        gid_local = gid[order]
+        g2l = np.full(self.n_global, -1, np.int64)
+        g2l[gid_local] = np.arange(n_local)
+        own_local = where[:self.gid.size]
+        h = self._local_handle(n_local)
+        try:
+            for k in ("pos", "vel", "omega", "radius", "mass"):
+                h.set(k, np.concatenate([self.f[k]] + [x[k] for x in halo])[order])
+            hp_own, hx_own = self._history_to_local(g2l)
+            hp = np.full((n_local, self.C), NO_PARTNER, np.uint32)
+            hx = np.zeros((n_local, self.C, 3))
+            hp[own_local] = hp_own
+            hx[own_local] = hx_own
+            h.set_dem_history(hp, hx)
+            h.step(1)
+            for k in ("pos", "vel", "omega"):
+                self.f[k] = np.asarray(h.get(k), np.float64).reshape(n_local, 3)[own_local].copy()
+            hp, hx = h.dem_history()
+            self.hpid = self._history_to_global(np.asarray(hp).reshape(n_local, self.C)[own_local], gid_local)
+            self.hxi = np.asarray(hx, np.float64).reshape(n_local, self.C, 3)[own_local].copy()
+        except BaseException:
+            self.close()
+            raise
+        # migration to the neighbour slabs, with the history
+        dest = self._owner(self.f["pos"][:, self.axis])
+        if np.any(np.abs(dest - self.rank) > 1):
+            raise RuntimeError("a sphere moved further than one slab in one step")
+        incoming = []
+        for peer in (self.rank - 1, self.rank + 1):
+            if 0 <= peer < self.world:
+                incoming.append(self._unpack(_exchange(self.dist, peer, self._rows(dest == peer, True)), True))
+        keep = dest == self.rank
+        self.gid = np.concatenate([self.gid[keep]] + [m["gid"] for m in incoming])
+        for k in self.f:
+            self.f[k] = np.concatenate([self.f[k][keep]] + [m[k] for m in incoming])
+        self.hpid = np.concatenate([self.hpid[keep]] + [m["hpid"] for m in incoming])
+        self.hxi = np.concatenate([self.hxi[keep]] + [m["hxi"] for m in incoming])
+        o = np.argsort(self.gid, kind="stable")
+        self.gid = self.gid[o]
+        for k in self.f:
+            self.f[k] = self.f[k][o]
+        self.hpid, self.hxi = self.hpid[o], self.hxi[o]
+
+    def _local_handle(self, n_local):
+        if self._handle is not None and self._handle_n == n_local:
+            return self._handle
+        self.close()
+        self._handle = self.make_handle(dict(self.cfg), n_local)
+        self._handle_n = n_local
+        return self._handle
+
+    def close(self):
+        if self._handle is not None:
+            self._handle.close()
+        self._handle = None
+        self._handle_n = None
+
+    def run(self, nsteps):
+        for _ in range(nsteps):
+            self.step()
+
+    def gather(self):
+        """The whole system's pos, vel, omega and history (global ids) in global-id order, on every
+        rank."""
+        parts = [None] * self.world
+        self.dist.all_gather_object(parts, (self.gid, self.f["pos"], self.f["vel"], self.f["omega"], self.hpid,
+                                            self.hxi))
+        gid = np.concatenate([p[0] for p in parts])
+        o = np.argsort(gid)
+        assert np.array_equal(gid[o], np.arange(self.n_global))
+        return tuple(np.concatenate([p[i] for p in parts])[o] for i in range(1, 6))

@@ -6,6 +6,9 @@ host logic alone: cut points, halo selection, the densities sent back between th
 migration and the global-id ordering of the local systems.  The slabs together must reproduce
 the single-domain oracle run bit for bit, with 2 and 3 ranks (the middle rank of 3 has two
 neighbours), on the 2D dam break (walls, particles crossing the cuts) and on a 3D lattice.
+The DEM slabs (SlabDEM, one oracle step per step) likewise, on a contact-dense lattice whose
+spheres cross the z cuts with their tangential history: positions, velocities, spins and the
+history (global ids) bit for bit.
 """
 import os
 import pickle
@@ -109,3 +112,101 @@ def test_slabs_reproduce_the_single_domain_run(oracle, tmp_path, world, name):
     assert all(min(x["counts"]) > 0 for x in ranks)  # every slab holds particles
     if name == "dam2d":  # particles crossed cuts: some rank's count changed during the run
         assert any(len(set(x["counts"])) > 1 for x in ranks)
+
+
+# ---- DEM slabs -------------------------------------------------------------------------------
+class OracleDemHandle:
+    """The calls SlabDEM makes on a DEM handle, computed by the oracle (f64)."""
+
+    def __init__(self, cfg, n):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import py_oracle
+        self.o = py_oracle
+        self.cfg = cfg
+        self.n = n
+        self.C = int(cfg.get("contact_capacity", 16))
+        self.f = {}
+        self.hp = np.full(n * self.C, 0xFFFFFFFF, np.uint32)
+        self.hx = np.zeros(n * self.C * 3)
+
+    def set(self, name, values):
+        self.f[name] = np.array(values, np.float64)
+
+    def get(self, name):
+        return self.f[name].copy()
+
+    def set_dem_history(self, pid, xi):
+        self.hp = np.array(pid, np.uint32).reshape(-1)
+        self.hx = np.array(xi, np.float64).reshape(-1)
+
+    def dem_history(self):
+        return self.hp.reshape(self.n, self.C).copy(), self.hx.reshape(self.n, self.C, 3).copy()
+
+    def step(self, nsteps=1):
+        st = self.o.DemState(self.f["pos"], self.f["vel"], self.f["omega"], self.f["radius"], self.f["mass"], self.C)
+        st.hpid[:] = self.hp
+        st.hxi[:] = self.hx
+        c, _ = self.o.dem_run(self.cfg, st, nsteps)
+        assert c >= 0, "contact slots overflowed"
+        self.f["pos"], self.f["vel"], self.f["omega"] = st.pos, st.vel, st.omega
+        self.hp, self.hx = st.hpid.copy(), st.hxi.copy()
+
+    def close(self):
+        pass
+
+
+def _dem_case():
+    """A contact-dense lattice whose spheres move fast along z (the cut axis), so that spheres
+    cross the cuts with their contact history within a few steps."""
+    sys.path.insert(0, ROOT)
+    from prestige_gb300 import workloads
+    w = workloads.dem_compressed_lattice(nside=(4, 4, 14), seed=2)
+    w["config"]["dt"] = 2e-6
+    w["fields"]["vel"][:, 2] = np.random.default_rng(5).normal(0.0, 40.0, size=w["n"])
+    return w, 10
+
+
+def _dem_worker(rank, world, port, out):
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port),
+                      CUDA_VISIBLE_DEVICES="", OMP_NUM_THREADS="1")
+    sys.path.insert(0, ROOT)
+    import torch.distributed as dist
+    from prestige_gb300.slab import SlabDEM
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    w, nsteps = _dem_case()
+    slab = SlabDEM(w["config"], w["fields"], dist, axis=2, make_handle=OracleDemHandle)
+    owned = []
+    for _ in range(nsteps):
+        slab.step()
+        owned.append(hash(slab.gid.tobytes()))
+    slab.close()
+    res = slab.gather()
+    if rank == 0:
+        with open(out, "wb") as f:
+            pickle.dump(res, f)
+    with open(out + ".r%d" % rank, "wb") as f:
+        pickle.dump({"owned": owned}, f)
+    dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_dem_slabs_reproduce_the_single_domain_run(oracle, tmp_path, world):
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    out = str(tmp_path / "slabdem.pkl")
+    mp.start_processes(_dem_worker, args=(world, _free_port(), out), nprocs=world, join=True, start_method="spawn")
+    with open(out, "rb") as f:
+        pos, vel, omega, hpid, hxi = pickle.load(f)
+    w, nsteps = _dem_case()
+    f = w["fields"]
+    C = w["config"]["contact_capacity"]
+    st = oracle.DemState(f["pos"], f["vel"], f["omega"], f["radius"], f["mass"], C)
+    c, _ = oracle.dem_run(w["config"], st, nsteps)
+    assert c > 0
+    assert np.array_equal(pos, st.pos) and np.array_equal(vel, st.vel) and np.array_equal(omega, st.omega)
+    assert np.array_equal(hpid.reshape(-1), st.hpid) and np.array_equal(hxi.reshape(-1), st.hxi)
+    owned = []
+    for r in range(world):
+        with open(out + ".r%d" % r, "rb") as fh:
+            owned.append(pickle.load(fh)["owned"])
+    assert any(len(set(x)) > 1 for x in owned)  # spheres crossed cuts during the run

@@ -8,6 +8,8 @@
     exchange; no kernel of one rank waits on the other) run the slab decomposition of
     prestige_gb300/slab.py: in the IEEE mode the slabs reproduce the single-domain oracle run bit
     for bit, in the double-word mode within 1e-10.
+  * Two DEM slabs (SlabDEM, cut along z, spheres crossing it with their contact history) reproduce
+    the single-domain oracle run bit for bit, history included.
 """
 import os
 import pickle
@@ -134,3 +136,44 @@ def test_two_slabs_on_the_gpu(pg, oracle, tmp_path, mode):
     else:
         rel = lambda a, b: np.abs(a - b).max() / np.abs(b).max()
         assert rel(pos, st.pos) <= 1e-10 and rel(vel, st.vel) <= 1e-10 and rel(rho, st.rho) <= 1e-10
+
+
+def _dem_case():
+    w = workloads.dem_compressed_lattice(nside=(4, 4, 14), seed=2)
+    w["config"]["dt"] = 2e-6
+    w["fields"]["vel"][:, 2] = np.random.default_rng(5).normal(0.0, 40.0, size=w["n"])
+    return w, 10
+
+
+def _dem_rank(rank, world, port, out):
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    sys.path.insert(0, ROOT)
+    import torch.distributed as dist
+    from prestige_gb300.slab import SlabDEM
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    w, nsteps = _dem_case()
+    slab = SlabDEM(w["config"], w["fields"], dist, axis=2)
+    slab.run(nsteps)
+    slab.close()
+    res = slab.gather()
+    if rank == 0:
+        with open(out, "wb") as f:
+            pickle.dump(res, f)
+    dist.destroy_process_group()
+
+
+def test_two_dem_slabs_on_the_gpu(pg, oracle, tmp_path):
+    """Two DEM slabs (z cut, spheres crossing it with their contact history) on two GPU ranks
+    reproduce the single-domain oracle run bit for bit, history included."""
+    import torch.multiprocessing as mp
+    out = str(tmp_path / "slabdem.pkl")
+    mp.start_processes(_dem_rank, args=(2, _free_port(), out), nprocs=2, join=True, start_method="spawn")
+    with open(out, "rb") as f:
+        pos, vel, omega, hpid, hxi = pickle.load(f)
+    w, nsteps = _dem_case()
+    f = w["fields"]
+    st = oracle.DemState(f["pos"], f["vel"], f["omega"], f["radius"], f["mass"], w["config"]["contact_capacity"])
+    c, _ = oracle.dem_run(w["config"], st, nsteps)
+    assert c > 0
+    assert np.array_equal(pos, st.pos) and np.array_equal(vel, st.vel) and np.array_equal(omega, st.omega)
+    assert np.array_equal(hpid.reshape(-1), st.hpid) and np.array_equal(hxi.reshape(-1), st.hxi)
