@@ -146,8 +146,11 @@ int ensure_sorted_buffers(pg_system* s) {
   for (int i = 0; i < 6; ++i)
     if (sz[i]) PG_TRY(s->sorted[i].ensure(sz[i] * (n + kPackPad)));
   PG_TRY(s->nlist.ensure(4 * ((n + kListTile - 1) / kListTile) * kListTile * (size_t)s->list_cap));
-  if (s->arith == ARITH_F64_DF)
-    PG_TRY(s->fcache.ensure(16 * ((n + kListTile - 1) / kListTile) * kListTile * (size_t)s->list_cap));
+  // per list entry: {m_j F, u} (double-word, 16 B) or F, w and r^2 + eps h^2 (IEEE double, 24 B),
+  // written by the continuity pass and read by the momentum pass of the same step
+  const size_t entries = ((n + kListTile - 1) / kListTile) * kListTile * (size_t)s->list_cap;
+  if (s->arith == ARITH_F64_DF) PG_TRY(s->fcache.ensure(16 * entries));
+  if (s->arith == ARITH_F64_EXACT) PG_TRY(s->fcache.ensure(24 * entries));
   PG_TRY(s->nlen.ensure(4 * n));
   PG_TRY(s->nresume.ensure(8 * n));
   PG_TRY(s->posmin.ensure(3 * sizeof(unsigned long long) * (size_t)s->nsys));
@@ -177,7 +180,7 @@ SphArgs sph_args(pg_system* s, int integrate, bool rates) {
   a.nlist = s->nlist.as<uint32_t>();
   a.nlen = s->nlen.as<uint32_t>();
   a.nresume = s->nresume.as<uint32_t>();
-  a.fcache = s->arith == ARITH_F64_DF ? s->fcache.p : nullptr;
+  a.fcache = s->arith == ARITH_F64_DF || s->arith == ARITH_F64_EXACT ? s->fcache.p : nullptr;
   a.cap = (uint32_t)s->list_cap;
   a.err = s->err.as<unsigned>();
   a.posmin = s->posmin.as<unsigned long long>();

@@ -82,7 +82,8 @@ struct SphArgs {
                              // nlist[(k / 32) * cap * 32 + q * 32 + k % 32] (q < min(nlen[k], cap))
   uint32_t* nlen;            // neighbours of slot k that passed the prefilter (may exceed cap)
   uint32_t* nresume;         // (row, slot) where the walk continues when nlen[k] > cap
-  void* fcache;              // double-word mode: F (hi, lo) per list entry, same tiling as nlist
+  void* fcache;              // per list entry, same tiling as nlist: double-word mode {m_j F, u} (hi, lo);
+                             // IEEE double: planes of F, w and r^2 + eps h^2
   uint32_t cap;
   uint32_t k_begin, k_end;   // sorted slots handled by the list and pair kernels (k_begin a multiple
                              // of the block size; the whole system is [0, n))

@@ -61,7 +61,7 @@ struct pg_system {
   cudaStream_t aux = nullptr;
   cudaEvent_t ov_ev[2] = {nullptr, nullptr};
   pg::DevBuf nlist, nlen, nresume;
-  pg::DevBuf fcache;             // double-word mode: F per list entry (continuity -> momentum)
+  pg::DevBuf fcache;             // f64 modes: pair values per list entry (continuity -> momentum)
   pg::DevBuf posmin;             // 3 x u64, double-word mode (pos_min_kernel)
 
   // DEM contact history, id order, double buffered
