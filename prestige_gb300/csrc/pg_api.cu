@@ -146,11 +146,11 @@ int ensure_sorted_buffers(pg_system* s) {
   for (int i = 0; i < 6; ++i)
     if (sz[i]) PG_TRY(s->sorted[i].ensure(sz[i] * (n + kPackPad)));
   PG_TRY(s->nlist.ensure(4 * ((n + kListTile - 1) / kListTile) * kListTile * (size_t)s->list_cap));
-  // per list entry: {m_j F, u} (double-word, 16 B) or F, w and r^2 + eps h^2 (IEEE double, 24 B),
-  // written by the continuity pass and read by the momentum pass of the same step
+  // per list entry: {m_j F, u} (double-word, 16 B, written by the continuity pass and read by the
+  // momentum pass of the same step) or the pair values of the IEEE step (pg_sph_sym.cu)
   const size_t entries = ((n + kListTile - 1) / kListTile) * kListTile * (size_t)s->list_cap;
   if (s->arith == ARITH_F64_DF) PG_TRY(s->fcache.ensure(16 * entries));
-  if (s->arith == ARITH_F64_EXACT) PG_TRY(s->fcache.ensure(24 * entries));
+  if (s->arith == ARITH_F64_EXACT) PG_TRY(s->fcache.ensure(sph_sym_entry_bytes() * entries));
   PG_TRY(s->nlen.ensure(4 * n));
   PG_TRY(s->nresume.ensure(8 * n));
   PG_TRY(s->posmin.ensure(3 * sizeof(unsigned long long) * (size_t)s->nsys));
@@ -237,6 +237,17 @@ int enqueue_sph_front(pg_system* s, cudaEvent_t* ev) {
   SphArgs a = sph_args(s, 1, false);
   PG_TRY(launch_sph_gather(s->stream, a, s->arith));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[2], s->stream));
+  if (s->arith == ARITH_F64_EXACT) {
+    // each pair once (pg_sph_sym.cu): the pair values of a slot need its partners' complete lists
+    PG_TRY(launch_sph_list(s->stream, a, s->arith, s->list_grid, s->block));
+    s->list_arith = s->arith;
+    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
+    PG_TRY(launch_sph_sym(s->stream, a, 0, s->block));
+    PG_TRY(launch_sph_sym(s->stream, a, 1, s->block));
+    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
+    s->launches += neighbor_launches(s) + 4;
+    return PG_OK;
+  }
   if (s->ov_split > 0 && s->ov_split < s->n) {
     // lists of [0, split) first; then the continuity pass over them runs beside the lists of
     // [split, n) on the auxiliary stream, which goes on with the continuity pass over
@@ -272,6 +283,13 @@ int enqueue_sph_front(pg_system* s, cudaEvent_t* ev) {
 // update).  ev (optional): event 5 of a step (end).
 int enqueue_sph_momentum(pg_system* s, cudaEvent_t* ev) {
   SphArgs a = sph_args(s, 1, false);
+  if (s->arith == ARITH_F64_EXACT) {
+    PG_TRY(launch_sph_sym(s->stream, a, 2, mom_block(s)));
+    PG_TRY(launch_sph_sym(s->stream, a, 3, mom_block(s)));
+    s->launches += 2;
+    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[5], s->stream));
+    return PG_OK;
+  }
   PG_TRY(launch_sph_list_pass(s->stream, a, s->arith, SPH_MOM, s->pass_grid[SPH_MOM], mom_block(s), s->lanes));
   s->launches += 1;
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[5], s->stream));

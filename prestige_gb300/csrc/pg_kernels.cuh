@@ -106,6 +106,12 @@ int sph_list_regs(int arith, int dim, int stage, int lanes = 1);  // registers p
 int sph_list_occupancy(int arith, int dim, int stage, int block, int lanes = 1);  // stage < 0: the list kernel
 // The list kernel with an explicit FP32 prefilter-position pack a.s[pf_index] (conservative test).
 int launch_sph_list_pf(cudaStream_t st, const SphArgs& a, int pf_index, int grid, int block);
+// The IEEE f64 step with each neighbour pair evaluated once (pg_sph_sym.cu), over complete lists:
+// part 0 and 1 the continuity pass (pair values, then the sums, rho' and the {rho', P'} pack),
+// part 2 and 3 the momentum pass (pair values, then the sums and the update).  a.fcache holds
+// sph_sym_entry_bytes() per list entry.
+int launch_sph_sym(cudaStream_t st, const SphArgs& a, int part, int block);
+size_t sph_sym_entry_bytes();
 
 // Adjoint of one SPH step (pg_adjoint.cu).  s[0..4] hold the slot-ordered packs written by
 // launch_adjoint_prep; pos/vel/rho/mass are the state before the step (id order).

@@ -28,8 +28,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <type_traits>
-
 #include "pg_arith.cuh"
 #include "pg_internal.cuh"
 #include "pg_kernels.cuh"
@@ -199,24 +197,12 @@ struct RealPairs {
   SphC<R> c;
   R xi[3], vi[3], rhoi, Pi;
   R acc[3], dr;
-  // IEEE double, continuity and momentum passes of a step: the continuity pass stores, per list
-  // entry, the pair's F, w and r^2 + eps h^2 (the oracle's intermediate values) in three planes
-  // of the tiled list layout, and the momentum pass reads them instead of recomputing the square
-  // root and the spline's division (positions and velocities do not change between the two
-  // passes; the stored values are the recomputed ones, bit for bit).
-  static constexpr bool kCache = std::is_same<Ops, OpsD>::value && (STAGE == SPH_CONT || STAGE == SPH_MOM);
-  double* fc = nullptr;  // entry q of the slot: fc[q * kListTile], plane p at + p * plane
-  size_t plane = 0;
 
   __device__ __forceinline__ void begin(const SphArgs& a, const SphK& K, uint32_t k) {
     A = (const R4*)a.s[0];
     B = (const R4*)a.s[1];
     Q = (const R2*)a.s[2];
     c = consts<R>(K);
-    if (kCache && a.fcache) {
-      plane = (size_t)((a.n + kListTile - 1) / kListTile) * kListTile * a.cap;
-      fc = (double*)a.fcache + list_base(k, a.cap);
-    }
     const R4 Ai = A[k], Bi = B[k];
     xi[0] = Ai.x; xi[1] = Ai.y; xi[2] = Ai.z;
     vi[0] = Bi.x; vi[1] = Bi.y; vi[2] = Bi.z;
@@ -230,100 +216,58 @@ struct RealPairs {
     dr = R(0);
   }
 
-  // The neighbour's pack records (and, for a cached momentum pass, the entry's stored values),
-  // loaded ahead of its pair terms.
+  // The neighbour's pack records, loaded ahead of its pair terms.
   struct Pre {
     R4 a, b;
     R2 q;
-    R cF, cW, cR;
   };
   static constexpr bool kPrefetch = true;
 
-  __device__ __forceinline__ Pre fetch(uint32_t t, uint32_t q) const { return fetch_entry(t, q, STAGE == SPH_MOM && fc); }
-
-  // the momentum pass's stored entries are a DRAM stream like the lists (sph_list_pass_kernel)
-  static constexpr bool kL2Entry = kCache && STAGE == SPH_MOM;
-  __device__ __forceinline__ void prefetch_entry(uint32_t q) const {
-    if (fc) {
-      const double* e = fc + (size_t)q * kListTile;
-      prefetch_l2(e);
-      prefetch_l2(e + plane);
-      prefetch_l2(e + 2 * plane);
-    }
-  }
-
-  // cached: entry q of a momentum pass that takes F, w and r^2 + eps h^2 from the continuity pass
-  // (it then needs no velocities of the neighbour)
-  __device__ __forceinline__ Pre fetch_entry(uint32_t t, uint32_t q, bool cached) const {
+  __device__ __forceinline__ Pre fetch(uint32_t t, uint32_t) const {
     Pre p;
     p.a = A[t];
-    if (cached) {
-      const double* e = fc + (size_t)q * kListTile;
-      p.cF = e[0];
-      p.cW = e[plane];
-      p.cR = e[2 * plane];
-    } else {
-      p.b = B[t];
-    }
+    p.b = B[t];
     if (kMom) p.q = Q[t];
     return p;
   }
 
   // A candidate of the continued walk of an overflowed list (a superset: EXACT_TEST repeats the
-  // oracle's test); everything computed here.
-  __device__ __forceinline__ void pair(uint32_t t) { terms<EXACT_TEST, false>(t, 0, fetch_entry(t, 0, false)); }
+  // oracle's test).
+  __device__ __forceinline__ void pair(uint32_t t) { terms<EXACT_TEST>(t, fetch(t, 0)); }
 
   // A list entry: the lists hold exactly the oracle's neighbours in every mode (f64 lists are
   // classified with the f64 test, f32 lists with the IEEE FP32 test), so no test is repeated.
-  __device__ __forceinline__ void pair_with(uint32_t t, uint32_t q, const Pre& p) {
-    if (kCache && STAGE == SPH_MOM && fc) terms<false, true>(t, q, p);
-    else terms<false, false>(t, q, p);
-  }
+  __device__ __forceinline__ void pair_with(uint32_t t, uint32_t, const Pre& p) { terms<false>(t, p); }
 
-  template <bool TEST, bool CACHED>
-  __device__ __forceinline__ void terms(uint32_t t, uint32_t qe, const Pre& p) {
-    constexpr bool kStore = kCache && STAGE == SPH_CONT && !TEST;  // list entries of the continuity pass
+  template <bool TEST>
+  __device__ __forceinline__ void terms(uint32_t t, const Pre& p) {
     const R4 Aj = p.a;
     const R d0 = Ops::sub(xi[0], Aj.x), d1 = Ops::sub(xi[1], Aj.y);
     const R d2 = DIM == 3 ? Ops::sub(xi[2], Aj.z) : R(0);
-    R F, w, r2e;
-    if (CACHED) {
-      F = p.cF;
-      w = p.cW;
-      r2e = p.cR;
-    } else {
-      R r2 = Ops::add(Ops::mul(d0, d0), Ops::mul(d1, d1));
-      if (DIM == 3) r2 = Ops::add(r2, Ops::mul(d2, d2));
-      if (TEST) {
-        if (!(r2 < c.four_h2)) return;
-        if (!(r2 > R(0))) return;
-      }
-      const R4 Bj = p.b;
-      const R r = Ops::sqrt(r2);
-      const R q = Ops::mul(r, c.inv_h);
-      // both pieces of the spline in the oracle's operation order, then a select (no divergence;
-      // the selected value is bit for bit the oracle's)
-      const R tq = Ops::sub(R(2), q);
-      const R Fnear = Ops::mul(c.fa, Ops::sub(Ops::mul(R(2.25), q), R(3)));
-      const R Ffar = Ops::div(Ops::mul(c.fb, Ops::mul(tq, tq)), r);
-      F = q < R(1) ? Fnear : Ffar;
-      const R dv0 = Ops::sub(vi[0], Bj.x), dv1 = Ops::sub(vi[1], Bj.y);
-      const R dv2 = DIM == 3 ? Ops::sub(vi[2], Bj.z) : R(0);
-      w = Ops::add(Ops::mul(dv0, d0), Ops::mul(dv1, d1));
-      if (DIM == 3) w = Ops::add(w, Ops::mul(dv2, d2));
-      r2e = (kMom || kStore) ? Ops::add(r2, c.eps_h2) : R(0);
-      if (kStore && fc) {
-        double* e = fc + (size_t)qe * kListTile;
-        e[0] = F;
-        e[plane] = w;
-        e[2 * plane] = r2e;
-      }
+    R r2 = Ops::add(Ops::mul(d0, d0), Ops::mul(d1, d1));
+    if (DIM == 3) r2 = Ops::add(r2, Ops::mul(d2, d2));
+    if (TEST) {
+      if (!(r2 < c.four_h2)) return;
+      if (!(r2 > R(0))) return;
     }
+    const R4 Bj = p.b;
+    const R r = Ops::sqrt(r2);
+    const R q = Ops::mul(r, c.inv_h);
+    // both pieces of the spline in the oracle's operation order, then a select (no divergence;
+    // the selected value is bit for bit the oracle's)
+    const R tq = Ops::sub(R(2), q);
+    const R Fnear = Ops::mul(c.fa, Ops::sub(Ops::mul(R(2.25), q), R(3)));
+    const R Ffar = Ops::div(Ops::mul(c.fb, Ops::mul(tq, tq)), r);
+    const R F = q < R(1) ? Fnear : Ffar;
+    const R dv0 = Ops::sub(vi[0], Bj.x), dv1 = Ops::sub(vi[1], Bj.y);
+    const R dv2 = DIM == 3 ? Ops::sub(vi[2], Bj.z) : R(0);
+    R w = Ops::add(Ops::mul(dv0, d0), Ops::mul(dv1, d1));
+    if (DIM == 3) w = Ops::add(w, Ops::mul(dv2, d2));
     const R mj = Aj.w;
     if (kCont) dr = Ops::add(dr, Ops::mul(mj, Ops::mul(w, F)));
     if (kMom) {
       const R2 qj = p.q;
-      const R av = Ops::div(Ops::mul(c.avk, w), Ops::mul(r2e, Ops::add(rhoi, qj.x)));
+      const R av = Ops::div(Ops::mul(c.avk, w), Ops::mul(Ops::add(r2, c.eps_h2), Ops::add(rhoi, qj.x)));
       const R pij = w < R(0) ? av : R(0);
       const R coef = Ops::mul(mj, Ops::mul(Ops::add(Ops::add(Pi, qj.y), pij), F));
       acc[0] = Ops::sub(acc[0], Ops::mul(coef, d0));
