@@ -62,12 +62,13 @@ struct pg_adjoint {
   pg::DevBuf seg_cell, seg_id, seg_start;
   pg::DevBuf lx, lv, lr, ga, gb;
   pg::DevBuf X4, V4, Q4, A4, PF, DB;  // slot-ordered packs of one adjoint step
+  pg::DevBuf EP, PS;                  // FP64 adjoint: per-entry pair values, per-slot partial sums
   int pass_grid[3] = {0, 0, 0};
   int pass_grid_fp32 = -1;
   size_t bytes() const {
     const pg::DevBuf* b[] = {&ckpt, &final_state, &seg_state, &seg_rnext, &seg_cell, &seg_id, &seg_start,
                              &lx,   &lv,          &lr,        &ga,        &gb,       &X4,     &V4,
-                             &Q4,   &A4,          &PF,        &DB};
+                             &Q4,   &A4,          &PF,        &DB,       &EP,     &PS};
     size_t t = 0;
     for (const pg::DevBuf* d : b) t += d->bytes;
     return t;
@@ -698,14 +699,19 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
     a.s[5] = A->A4.p;
     a.s[6] = A->DB.p;
     a.s[7] = nullptr;
-  } else {
+  } else {  // each pair once (pg_adjoint_sym.cu): entry planes and per-slot partial sums
+    const size_t entries = ((nn + pg::kListTile - 1) / pg::kListTile) * pg::kListTile * (size_t)s->list_cap;
+    PG_TRY(A->EP.ensure(pg::adjoint_sym_entry_bytes() * entries));
+    PG_TRY(A->PS.ensure(pg::adjoint_sym_slot_bytes() * nn));
     a.s[0] = A->X4.p;
     a.s[1] = A->V4.p;
     a.s[2] = A->Q4.p;
     a.s[3] = A->A4.p;
     a.s[4] = A->PF.p;
     a.s[5] = A->DB.p;
-    a.s[6] = a.s[7] = nullptr;
+    a.s[6] = A->PS.p;
+    a.s[7] = nullptr;
+    a.fcache = A->EP.p;
   }
   a.lam[0] = A->lx.p;
   a.lam[1] = A->lv.p;
@@ -741,9 +747,14 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
       a.sorted_id = A->seg_id.as<uint32_t>() + (size_t)t * n;
       a.cell_start = A->seg_start.as<uint32_t>() + (size_t)t * ncp1;
       PG_TRY(pg::launch_adjoint_prep(s->stream, a, fp32));
-      PG_TRY(pg::launch_sph_list_pf(s->stream, a, pg::adjoint_pf_index(fp32), 0, pg::kSphThreads));
-      PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_MOM, A->pass_grid[pg::SPH_MOM], fp32));
-      PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_CONT, A->pass_grid[pg::SPH_CONT], fp32));
+      if (fp32) {
+        PG_TRY(pg::launch_sph_list_pf(s->stream, a, pg::adjoint_pf_index(fp32), 0, pg::kSphThreads));
+        PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_MOM, A->pass_grid[pg::SPH_MOM], fp32));
+        PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_CONT, A->pass_grid[pg::SPH_CONT], fp32));
+      } else {
+        PG_TRY(pg::launch_sph_list_exact(s->stream, a, pg::adjoint_pf_index(fp32), 0, pg::kSphThreads));
+        for (int part = 0; part < 5; ++part) PG_TRY(pg::launch_adjoint_sym(s->stream, a, part));
+      }
     }
   }
   PG_TRY(pg::copy_state_in(s, A->final_state.as<double>()));

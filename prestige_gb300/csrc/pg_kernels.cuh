@@ -120,6 +120,16 @@ int launch_adjoint_prep(cudaStream_t st, const SphArgs& a, bool fp32);
 int launch_adjoint_pass(cudaStream_t st, const SphArgs& a, int stage, int grid, bool fp32);
 int adjoint_pass_occupancy(int dim, int stage, bool fp32);
 int adjoint_pf_index(bool fp32);
+// The FP64 adjoint passes with each pair evaluated once (pg_adjoint_sym.cu), over exact lists
+// (launch_sph_list_exact): part 0 the mirror indices, 1, 2 the momentum adjoint, 3, 4 the
+// continuity adjoint.
+// a.fcache: adjoint_sym_entry_bytes() per list entry; a.s[6]: adjoint_sym_slot_bytes() per slot.
+int launch_adjoint_sym(cudaStream_t st, const SphArgs& a, int part);
+size_t adjoint_sym_entry_bytes();
+size_t adjoint_sym_slot_bytes();
+// The list kernel with the f64 test of the exact neighbours on the double4 positions a.s[0] and
+// the FP32 prefilter positions a.s[pf_index].
+int launch_sph_list_exact(cudaStream_t st, const SphArgs& a, int pf_index, int grid, int block);
 // Bytes per particle of the sorted packed arrays s[0..5] for an arithmetic mode.
 void sph_sorted_layout(int arith, size_t sizes[6]);
 

@@ -684,6 +684,11 @@ int launch_sph_list_pf(cudaStream_t st, const SphArgs& a, int pf_index, int grid
   return launch_table(st, a, kern, pf_index, grid, block, 1);
 }
 
+int launch_sph_list_exact(cudaStream_t st, const SphArgs& a, int pf_index, int grid, int block) {
+  PassKernel kern = a.dim == 2 ? sph_list_kernel<2, false, 0> : sph_list_kernel<3, false, 0>;
+  return launch_table(st, a, kern, pf_index, grid, block, 1);
+}
+
 int launch_sph_list_pass(cudaStream_t st, const SphArgs& a, int arith, int stage, int grid, int block, int lanes) {
   int pf = 0;
   lanes = sph_pass_lanes(arith, stage, lanes);
