@@ -57,18 +57,36 @@ struct pg_adjoint {
   size_t state_doubles = 0;  // n * (2 dim + 1): pos, vel, rho
   pg::DevBuf ckpt;           // nseg states
   pg::DevBuf final_state;
-  pg::DevBuf seg_state;      // `every` states of the segment being swept
-  pg::DevBuf seg_rnext;      // rho' of each step of the segment
-  pg::DevBuf seg_cell, seg_id, seg_start;
+  // two segments' recomputed steps: one is swept (on `sweep`) while the previous segment is
+  // recomputed into the other (on the handle's stream)
+  pg::DevBuf seg_state[2];   // `every` states of a segment
+  pg::DevBuf seg_rnext[2];   // rho' of each step of the segment
+  pg::DevBuf seg_cell[2], seg_id[2], seg_start[2];
+  pg::DevBuf nlist, nlen, nresume;  // the sweep's neighbour lists (the recompute uses the handle's)
+  cudaStream_t sweep = nullptr;
+  cudaEvent_t ev_rec[2] = {nullptr, nullptr}, ev_sweep[2] = {nullptr, nullptr};
+  ~pg_adjoint() {
+    if (sweep) {
+      cudaStreamSynchronize(sweep);
+      cudaStreamDestroy(sweep);
+    }
+    for (int b = 0; b < 2; ++b) {
+      if (ev_rec[b]) cudaEventDestroy(ev_rec[b]);
+      if (ev_sweep[b]) cudaEventDestroy(ev_sweep[b]);
+    }
+  }
   pg::DevBuf lx, lv, lr, ga, gb;
   pg::DevBuf X4, V4, Q4, A4, PF, DB;  // slot-ordered packs of one adjoint step
   pg::DevBuf EP, PS;                  // FP64 adjoint: per-entry pair values, per-slot partial sums
   int pass_grid[3] = {0, 0, 0};
   int pass_grid_fp32 = -1;
   size_t bytes() const {
-    const pg::DevBuf* b[] = {&ckpt, &final_state, &seg_state, &seg_rnext, &seg_cell, &seg_id, &seg_start,
-                             &lx,   &lv,          &lr,        &ga,        &gb,       &X4,     &V4,
-                             &Q4,   &A4,          &PF,        &DB,       &EP,     &PS};
+    const pg::DevBuf* b[] = {&ckpt,         &final_state,  &seg_state[0], &seg_rnext[0], &seg_cell[0],
+                             &seg_id[0],    &seg_start[0], &seg_state[1], &seg_rnext[1], &seg_cell[1],
+                             &seg_id[1],    &seg_start[1], &nlist,        &nlen,         &nresume,
+                             &lx,           &lv,           &lr,           &ga,           &gb,
+                             &X4,           &V4,           &Q4,           &A4,           &PF,
+                             &DB,           &EP,           &PS};
     size_t t = 0;
     for (const pg::DevBuf* d : b) t += d->bytes;
     return t;
@@ -657,11 +675,24 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
   const size_t n = s->n, nn = n ? n : 1, nd = n * (size_t)s->dim;
   const size_t ncp1 = s->ncells + 1;
   const int every = A->every;
-  PG_TRY(A->seg_state.ensure(8 * A->state_doubles * every + 8));
-  PG_TRY(A->seg_rnext.ensure(8 * nn * every));
-  PG_TRY(A->seg_cell.ensure(4 * nn * every));
-  PG_TRY(A->seg_id.ensure(4 * nn * every));
-  PG_TRY(A->seg_start.ensure(4 * ncp1 * every));
+  for (int b = 0; b < 2; ++b) {
+    PG_TRY(A->seg_state[b].ensure(8 * A->state_doubles * every + 8));
+    PG_TRY(A->seg_rnext[b].ensure(8 * nn * every));
+    PG_TRY(A->seg_cell[b].ensure(4 * nn * every));
+    PG_TRY(A->seg_id[b].ensure(4 * nn * every));
+    PG_TRY(A->seg_start[b].ensure(4 * ncp1 * every));
+  }
+  const size_t list_entries = ((nn + pg::kListTile - 1) / pg::kListTile) * pg::kListTile * (size_t)s->list_cap;
+  PG_TRY(A->nlist.ensure(4 * list_entries));
+  PG_TRY(A->nlen.ensure(4 * nn));
+  PG_TRY(A->nresume.ensure(8 * nn));
+  if (!A->sweep) {
+    PG_CUDA_TRY(cudaStreamCreateWithFlags(&A->sweep, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; ++b) {
+      PG_CUDA_TRY(cudaEventCreateWithFlags(&A->ev_rec[b], cudaEventDisableTiming));
+      PG_CUDA_TRY(cudaEventCreateWithFlags(&A->ev_sweep[b], cudaEventDisableTiming));
+    }
+  }
   PG_TRY(A->lx.ensure(8 * nn * s->dim));
   PG_TRY(A->lv.ensure(8 * nn * s->dim));
   PG_TRY(A->lr.ensure(8 * nn));
@@ -718,45 +749,74 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
   a.lam[2] = A->lr.p;
   a.lam[3] = A->ga.p;
   a.lam[4] = A->gb.p;
+  a.nlist = A->nlist.as<uint32_t>();
+  a.nlen = A->nlen.as<uint32_t>();
+  a.nresume = A->nresume.as<uint32_t>();
+  if (fp32) a.fcache = nullptr;
 
-  for (int seg = A->nseg - 1; seg >= 0; --seg) {
+  // Segment seg recomputed into buffer set b on the handle's stream: the steps from the
+  // segment's checkpoint, keeping each step's state, rho' and neighbour structure.  It waits
+  // for the sweep that last read the set.
+  bool pending[2] = {false, false};
+  auto recompute = [&](int seg, int b) -> int {
+    if (pending[b]) PG_CUDA_TRY(cudaStreamWaitEvent(s->stream, A->ev_sweep[b], 0));
     const int steps = std::min(every, A->nsteps - seg * every);
-    // recompute the segment, keeping each step's state, rho' and neighbour structure
     PG_TRY(pg::copy_state_in(s, A->ckpt.as<double>() + (size_t)seg * A->state_doubles));
     for (int t = 0; t < steps; ++t) {
-      PG_TRY(pg::copy_state_out(s, A->seg_state.as<double>() + (size_t)t * A->state_doubles));
+      PG_TRY(pg::copy_state_out(s, A->seg_state[b].as<double>() + (size_t)t * A->state_doubles));
       PG_TRY(pg::enqueue_sph_step(s, false, 1, nullptr));
       if (n) {
-        PG_CUDA_TRY(cudaMemcpyAsync(A->seg_rnext.as<double>() + (size_t)t * n, s->rho.p, 8 * n,
+        PG_CUDA_TRY(cudaMemcpyAsync(A->seg_rnext[b].as<double>() + (size_t)t * n, s->rho.p, 8 * n,
                                     cudaMemcpyDeviceToDevice, s->stream));
-        PG_CUDA_TRY(cudaMemcpyAsync(A->seg_cell.as<uint32_t>() + (size_t)t * n, s->nw.sorted_cell, 4 * n,
+        PG_CUDA_TRY(cudaMemcpyAsync(A->seg_cell[b].as<uint32_t>() + (size_t)t * n, s->nw.sorted_cell, 4 * n,
                                     cudaMemcpyDeviceToDevice, s->stream));
-        PG_CUDA_TRY(cudaMemcpyAsync(A->seg_id.as<uint32_t>() + (size_t)t * n, s->nw.sorted_id, 4 * n,
+        PG_CUDA_TRY(cudaMemcpyAsync(A->seg_id[b].as<uint32_t>() + (size_t)t * n, s->nw.sorted_id, 4 * n,
                                     cudaMemcpyDeviceToDevice, s->stream));
       }
-      PG_CUDA_TRY(cudaMemcpyAsync(A->seg_start.as<uint32_t>() + (size_t)t * ncp1, s->nw.cell_start.p, 4 * ncp1,
+      PG_CUDA_TRY(cudaMemcpyAsync(A->seg_start[b].as<uint32_t>() + (size_t)t * ncp1, s->nw.cell_start.p, 4 * ncp1,
                                   cudaMemcpyDeviceToDevice, s->stream));
     }
-    // sweep the adjoint back through the segment
+    PG_CUDA_TRY(cudaEventRecord(A->ev_rec[b], s->stream));
+    return PG_OK;
+  };
+  // The adjoint swept back through segment seg (buffer set b) on the sweep stream, after its
+  // recompute (and, through the stream order of that recompute, after the setup above).  It
+  // touches none of the handle's buffers that a recompute writes.
+  auto sweep = [&](int seg, int b) -> int {
+    cudaStream_t st = A->sweep;
+    PG_CUDA_TRY(cudaStreamWaitEvent(st, A->ev_rec[b], 0));
+    const int steps = std::min(every, A->nsteps - seg * every);
     for (int t = steps - 1; t >= 0; --t) {
-      const double* st = A->seg_state.as<double>() + (size_t)t * A->state_doubles;
-      a.pos = (void*)st;
-      a.vel = (void*)(st + nd);
-      a.rho = (void*)(A->seg_rnext.as<double>() + (size_t)t * n);
-      a.sorted_cell = A->seg_cell.as<uint32_t>() + (size_t)t * n;
-      a.sorted_id = A->seg_id.as<uint32_t>() + (size_t)t * n;
-      a.cell_start = A->seg_start.as<uint32_t>() + (size_t)t * ncp1;
-      PG_TRY(pg::launch_adjoint_prep(s->stream, a, fp32));
+      const double* sv = A->seg_state[b].as<double>() + (size_t)t * A->state_doubles;
+      a.pos = (void*)sv;
+      a.vel = (void*)(sv + nd);
+      a.rho = (void*)(A->seg_rnext[b].as<double>() + (size_t)t * n);
+      a.sorted_cell = A->seg_cell[b].as<uint32_t>() + (size_t)t * n;
+      a.sorted_id = A->seg_id[b].as<uint32_t>() + (size_t)t * n;
+      a.cell_start = A->seg_start[b].as<uint32_t>() + (size_t)t * ncp1;
+      PG_TRY(pg::launch_adjoint_prep(st, a, fp32));
       if (fp32) {
-        PG_TRY(pg::launch_sph_list_pf(s->stream, a, pg::adjoint_pf_index(fp32), 0, pg::kSphThreads));
-        PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_MOM, A->pass_grid[pg::SPH_MOM], fp32));
-        PG_TRY(pg::launch_adjoint_pass(s->stream, a, pg::SPH_CONT, A->pass_grid[pg::SPH_CONT], fp32));
+        PG_TRY(pg::launch_sph_list_pf(st, a, pg::adjoint_pf_index(fp32), 0, pg::kSphThreads));
+        PG_TRY(pg::launch_adjoint_pass(st, a, pg::SPH_MOM, A->pass_grid[pg::SPH_MOM], fp32));
+        PG_TRY(pg::launch_adjoint_pass(st, a, pg::SPH_CONT, A->pass_grid[pg::SPH_CONT], fp32));
       } else {
-        PG_TRY(pg::launch_sph_list_exact(s->stream, a, pg::adjoint_pf_index(fp32), 0, pg::kSphThreads));
-        for (int part = 0; part < 5; ++part) PG_TRY(pg::launch_adjoint_sym(s->stream, a, part));
+        PG_TRY(pg::launch_sph_list_exact(st, a, pg::adjoint_pf_index(fp32), 0, pg::kSphThreads));
+        for (int part = 0; part < 5; ++part) PG_TRY(pg::launch_adjoint_sym(st, a, part));
       }
     }
+    PG_CUDA_TRY(cudaEventRecord(A->ev_sweep[b], st));
+    pending[b] = true;
+    return PG_OK;
+  };
+  // the recompute of the previous segment runs beside the sweep of this one
+  if (A->nseg > 0) PG_TRY(recompute(A->nseg - 1, 0));
+  for (int seg = A->nseg - 1; seg >= 0; --seg) {
+    const int b = (A->nseg - 1 - seg) & 1;
+    if (seg > 0) PG_TRY(recompute(seg - 1, b ^ 1));
+    PG_TRY(sweep(seg, b));
   }
+  for (int b = 0; b < 2; ++b)
+    if (pending[b]) PG_CUDA_TRY(cudaStreamWaitEvent(s->stream, A->ev_sweep[b], 0));
   PG_TRY(pg::copy_state_in(s, A->final_state.as<double>()));
   std::vector<double> ga(n), gb(n);
   if (n) {

@@ -12,12 +12,13 @@
 //           (binary search: the partner's list is ascending), or none.
 //   adj_a1  (entries above the slot) the momentum terms; its own share into per-slot partial
 //           sums; the partner's share (the vectors, F x.E and Pi / rho_ij) into the partner's list
-//           entry at the mirror index; G w and F of the pair
-//           into the slot's own entry for the continuity pass; the parameter derivatives of the
-//           pair whole (half of each when the partner evaluates its side itself).
+//           entry at the mirror index; the pair's continuity vectors U1 = G w x + F v and
+//           U2 = F x and the partner's mass into the slot's own entry; the parameter derivatives
+//           of the pair whole (half of each when the partner evaluates its side itself).
 //   adj_a2  (entries below the slot, in list order) the partners' shares, then the momentum
 //           update of lx, lv, lr, the parameter sums and dbar = dt lr for the continuity pass.
-//   adj_c1 / adj_c2  the same for the continuity terms (G w and F taken from adj_a1).
+//   adj_c1 / adj_c2  the same for the continuity terms: the slot's share is D U1 and D U2 with
+//           D = dbar_k m_t + dbar_t m_k (dbar from adj_a2), the partner's the negated vectors.
 // A pair that is not held by both lists (a list that reached its capacity) is evaluated by each
 // side for itself, as in the two-sided passes, with half of the parameter derivatives each; the
 // rest of an overflowed list's walk likewise.  The sums run in a different order from the
@@ -36,8 +37,10 @@ namespace {
 using namespace sphpass;
 
 constexpr uint32_t kNoMirror = 0xFFFFFFFFu;
-constexpr int kPlanes = 10;  // doubles per list entry (plus one u32)
-enum { kMx = 0, kMv = 3, kFxE = 6, kPIrb = 7, kGW = 8, kF = 9 };
+constexpr int kPlanes = 15;  // doubles per list entry (plus one u32)
+// the partner's momentum share (Vx, Vv, F x.E, Pi / rho_ij); for the continuity pass, the pair's
+// vectors U1 = G w x + F v and U2 = F x and the partner's mass (own entries above the slot)
+enum { kMx = 0, kMv = 3, kFxE = 6, kPIrb = 7, kU1 = 8, kU2 = 11, kMt = 14 };
 constexpr int kSlotSums = 9;  // per-slot partial sums: gx (3), gv (3), gr, gal, gB
 
 struct Planes {
@@ -151,7 +154,7 @@ __device__ __forceinline__ bool is_neighbor(const SphC<double>& c, const double4
 template <int DIM>
 struct MomTerms {
   double Vx[3], Vv[3], FxE, PIrb, gal, gB;  // gal, gB: the whole pair's parameter derivatives
-  double GW, F;
+  double U1[3], U2[3], mt;                  // the continuity share is D U1, D U2
 };
 
 template <int DIM>
@@ -164,7 +167,7 @@ __device__ __forceinline__ MomTerms<DIM> mom_terms(const SphK& K, const Packs& P
   const double rb = vk.w + vt.w;
   const double e = g.r2 + c.eps_h2;
   // one reciprocal serves the four quotients of the terms
-  const double inv_erb = 1.0 / (e * rb);
+  const double inv_erb = __drcp_rn(e * rb);
   const double inv_e = rb * inv_erb, inv_rb = e * inv_erb;
   double c1 = 0.0, c1a = 0.0;
   if (g.w < 0.0) {
@@ -191,8 +194,13 @@ __device__ __forceinline__ MomTerms<DIM> mom_terms(const SphK& K, const Packs& P
   m.PIrb = PI * inv_rb;
   m.gal = m.FxE * c1a * g.w;
   m.gB = m.FxE * (qk.z + qt.z);
-  m.GW = g.G * g.w;
-  m.F = g.F;
+  const double GW = g.G * g.w;
+#pragma unroll
+  for (int cc = 0; cc < 3; ++cc) {
+    m.U1[cc] = cc < DIM ? GW * g.d[cc] + g.F * g.dv[cc] : 0.0;
+    m.U2[cc] = cc < DIM ? g.F * g.d[cc] : 0.0;
+  }
+  m.mt = mt;
   return m;
 }
 
@@ -300,8 +308,12 @@ __global__ void __launch_bounds__(kSphMaxThreads) adj_a1_kernel(SphArgs a) {
     const uint32_t t = my[(size_t)q * kListTile];
     const MomTerms<DIM> m = mom_terms<DIM>(K, P, s.k, t, xk, vk);
     const size_t e = entry(s.k, q, a.cap);
-    E.at(kGW, e) = m.GW;
-    E.at(kF, e) = m.F;
+#pragma unroll
+    for (int cc = 0; cc < DIM; ++cc) {
+      E.at(kU1 + cc, e) = m.U1[cc];
+      E.at(kU2 + cc, e) = m.U2[cc];
+    }
+    E.at(kMt, e) = m.mt;
     const uint32_t mt = E.mirror(e);
     if (mt != kNoMirror) {
       const size_t f = entry(t, mt, a.cap);
@@ -367,32 +379,19 @@ __global__ void __launch_bounds__(kSphMaxThreads) adj_a2_kernel(SphArgs a) {
   ((double*)a.lam[4])[s.id] += sum.gB;
 }
 
-// The continuity-adjoint share of pair (k, t) from k's side, given G w and F of the pair.
-template <int DIM>
-__device__ __forceinline__ void cont_terms(const Packs& P, uint32_t k, uint32_t t, const double4_32a& xk,
-                                           const double4_32a& vk, double GW, double F, double* Vx, double* Vv) {
-  const double4_32a xt = P.X[t], vt = P.V[t];
-  const double D = P.DB[k] * xt.w + P.DB[t] * xk.w;
-  const double gw = GW * D, fd = F * D;
-  const double d[3] = {xk.x - xt.x, xk.y - xt.y, DIM == 3 ? xk.z - xt.z : 0.0};
-  const double dv[3] = {vk.x - vt.x, vk.y - vt.y, DIM == 3 ? vk.z - vt.z : 0.0};
-#pragma unroll
-  for (int cc = 0; cc < 3; ++cc) {
-    Vx[cc] = cc < DIM ? gw * d[cc] + fd * dv[cc] : 0.0;
-    Vv[cc] = cc < DIM ? fd * d[cc] : 0.0;
-  }
-}
-
+// The continuity-adjoint share of a pair from the slot's side is D U1 and D U2, with
+// D = dbar_k m_t + dbar_t m_k, U1 = G w x + F v and U2 = F x.
 template <int DIM>
 __device__ __forceinline__ void cont_full(const SphK& K, const Packs& P, uint32_t k, uint32_t t, const double4_32a& xk,
                                           const double4_32a& vk, Sums& sum) {
-  const Geo<DIM> g = geometry<DIM>(K.d, xk, vk, P.X[t], P.V[t]);
-  double Vx[3], Vv[3];
-  cont_terms<DIM>(P, k, t, xk, vk, g.G * g.w, g.F, Vx, Vv);
+  const double4_32a xt = P.X[t];
+  const Geo<DIM> g = geometry<DIM>(K.d, xk, vk, xt, P.V[t]);
+  const double D = P.DB[k] * xt.w + P.DB[t] * xk.w;
+  const double GW = g.G * g.w;
 #pragma unroll
   for (int cc = 0; cc < DIM; ++cc) {
-    sum.gx[cc] += Vx[cc];
-    sum.gv[cc] += Vv[cc];
+    sum.gx[cc] += D * (GW * g.d[cc] + g.F * g.dv[cc]);
+    sum.gv[cc] += D * (g.F * g.d[cc]);
   }
 }
 
@@ -402,7 +401,7 @@ __global__ void __launch_bounds__(kSphMaxThreads) adj_c1_kernel(SphArgs a) {
   if (!slot_of(a, s)) return;
   const Packs P(a);
   const Planes E = planes_of(a);
-  const double4_32a xk = P.X[s.k], vk = P.V[s.k];
+  const double mk = P.X[s.k].w, dbk = P.DB[s.k];
   const uint32_t* __restrict__ my = a.nlist + list_base(s.k, a.cap);
   Sums sum = {{0, 0, 0}, {0, 0, 0}, 0, 0, 0};
   // all lanes at the same entry index, so the entry-plane loads coalesce (this pass waits on its
@@ -411,10 +410,12 @@ __global__ void __launch_bounds__(kSphMaxThreads) adj_c1_kernel(SphArgs a) {
     const uint32_t t = my[(size_t)q * kListTile];
     if (t < s.k) continue;
     const size_t e = entry(s.k, q, a.cap);
-    double Vx[3], Vv[3];
-    cont_terms<DIM>(P, s.k, t, xk, vk, E.at(kGW, e), E.at(kF, e), Vx, Vv);
+    const double D = dbk * E.at(kMt, e) + P.DB[t] * mk;
+    double Vx[3] = {0, 0, 0}, Vv[3] = {0, 0, 0};
 #pragma unroll
     for (int cc = 0; cc < DIM; ++cc) {
+      Vx[cc] = D * E.at(kU1 + cc, e);
+      Vv[cc] = D * E.at(kU2 + cc, e);
       sum.gx[cc] += Vx[cc];
       sum.gv[cc] += Vv[cc];
     }
