@@ -37,7 +37,9 @@
 // walks the segments last to first; for each it restores the checkpoint, re-runs the forward
 // steps while keeping each step's state, its updated density and its neighbour structure
 // (sorted cells, sorted ids, cell table: integer data, reused as is), then sweeps the adjoint
-// back through the segment.  Memory: (nsteps / every) checkpoints plus one segment.
+// back through the segment.  The recompute of the previous segment runs beside the sweep (the
+// handle's stream and a second one), so two segments are held.  Memory: (nsteps / every)
+// checkpoints plus two segments.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
