@@ -110,8 +110,8 @@ def test_adjoint_matches_finite_differences(pg, mode):
         assert abs(dv0[i, c] - fd) <= FD_TOL * scale, (i, c, dv0[i, c], fd)
 
 
-def _dual_check(oracle, w, nsteps, every, mode=0):
-    da, dB, dv0, _, _, cfg = _gradients(w, nsteps, every, f64_mode=mode)
+def _dual_check(oracle, w, nsteps, every, mode=0, **over):
+    da, dB, dv0, _, _, cfg = _gradients(w, nsteps, every, f64_mode=mode, **over)
     tol = DUAL_TOL if mode == 0 else FD_TOL
     rng = np.random.default_rng(7)
     u = rng.normal(size=w["fields"]["vel"].shape)
@@ -137,6 +137,16 @@ def test_adjoint_matches_dual_number_oracle_2d_walls(pg, oracle, mode):
     w["fields"]["vel"][w["n_fluid"]:] = 0.0
     w["target"] = w["fields"]["pos"] + rng.normal(0.0, 0.002, size=w["fields"]["pos"].shape)
     _dual_check(oracle, w, nsteps=15, every=4, mode=mode)
+
+
+@pytest.mark.parametrize("cap", [16, 48])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_adjoint_with_lists_cut_short_matches_dual_numbers(pg, oracle, mode, cap):
+    """Neighbour lists shorter than the neighbour count: the FP64 adjoint's pairs that only one
+    list holds are evaluated by each side for itself, and the rest of each list's walk likewise
+    (16 entries cut every list among the lower slots, 48 among the upper ones); the mixed adjoint
+    follows its lists' continued walks.  The gradients stay within the dual-number bars."""
+    _dual_check(oracle, _small_3d(), nsteps=8, every=3, mode=mode, list_capacity=cap)
 
 
 def test_checkpoint_interval_does_not_change_gradients(pg):
