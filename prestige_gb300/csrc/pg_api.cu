@@ -237,6 +237,28 @@ int enqueue_sph_front(pg_system* s, cudaEvent_t* ev) {
   SphArgs a = sph_args(s, 1, false);
   PG_TRY(launch_sph_gather(s->stream, a, s->arith));
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[2], s->stream));
+  if (s->arith == ARITH_F64_EXACT && s->ov_split > 0 && s->ov_split < s->n) {
+    // each pair once (pg_sph_sym.cu); the lists of [split, n) on the auxiliary stream beside the
+    // lists of [0, split), then the pair values of the slots whose partners all lie below split,
+    // the rest once every list is built
+    SphArgs a1 = a, a2 = a;
+    a1.k_end = s->ov_split;
+    a2.k_begin = s->ov_split;
+    PG_CUDA_TRY(cudaEventRecord(s->ov_ev[0], s->stream));
+    PG_CUDA_TRY(cudaStreamWaitEvent(s->aux, s->ov_ev[0], 0));
+    PG_TRY(launch_sph_list(s->aux, a2, s->arith, s->ov_list_grid, s->block));
+    PG_CUDA_TRY(cudaEventRecord(s->ov_ev[1], s->aux));
+    PG_TRY(launch_sph_list(s->stream, a1, s->arith, s->list_grid, s->block));
+    s->list_arith = s->arith;
+    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[3], s->stream));
+    PG_TRY(launch_sph_sym(s->stream, a1, 0, s->block, s->ov_split, 0));
+    PG_CUDA_TRY(cudaStreamWaitEvent(s->stream, s->ov_ev[1], 0));
+    PG_TRY(launch_sph_sym(s->stream, a, 0, s->block, s->ov_split, 1));
+    PG_TRY(launch_sph_sym(s->stream, a, 1, s->block));
+    if (ev) PG_CUDA_TRY(cudaEventRecord(ev[4], s->stream));
+    s->launches += neighbor_launches(s) + 6;
+    return PG_OK;
+  }
   if (s->arith == ARITH_F64_EXACT) {
     // each pair once (pg_sph_sym.cu): the pair values of a slot need its partners' complete lists
     PG_TRY(launch_sph_list(s->stream, a, s->arith, s->list_grid, s->block));
@@ -512,8 +534,32 @@ int capture_graphs(pg_system* s) {
 // At 1M particles it is even (1.965 ms either way), at 256k slower (0.690 against 0.670 ms),
 // hence the threshold.  The 512-system batch of 2D dam breaks (6.1M particles, one handle)
 // gains too: 3.36 against 3.45 ms (with persistent grids it had lost, 3.91 against 3.81).
+// The auxiliary stream of the overlapped schedules (greatest priority: the list kernel's blocks
+// are placed first, the pair pass beside it fills the rest) and its two events.
+int ensure_aux_stream(pg_system* s) {
+  if (!s->aux) {
+    int least = 0, greatest = 0;
+    PG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    PG_CUDA_TRY(cudaStreamCreateWithPriority(&s->aux, cudaStreamNonBlocking, greatest));
+  }
+  for (int i = 0; i < 2; ++i)
+    if (!s->ov_ev[i]) PG_CUDA_TRY(cudaEventCreateWithFlags(&s->ov_ev[i], cudaEventDisableTiming));
+  return PG_OK;
+}
+
 int choose_overlap(pg_system* s, int sms) {
   s->ov_split = 0;
+  if (s->model == PG_MODEL_SPH && s->arith == ARITH_F64_EXACT && s->n >= 1000000) {
+    // IEEE step: the lists of the last three quarters of the slots (ALU work) beside the pair
+    // values (FP64 work) of the slots of the first quarter whose partners all lie in it
+    const int locc = sph_list_occupancy(s->arith, s->dim, -1, s->block);
+    if (locc < 1) return PG_OK;
+    PG_TRY(ensure_aux_stream(s));
+    s->ov_pass_grid = 0;
+    s->ov_list_grid = std::max(1, locc / 2) * sms;
+    s->ov_split = (uint32_t)(s->n / 4 / (size_t)s->block * (size_t)s->block);
+    return PG_OK;
+  }
   if (s->model != PG_MODEL_SPH || s->arith != ARITH_F64_DF || s->n < 1000000) return PG_OK;
   const int rp = sph_list_regs(s->arith, s->dim, SPH_CONT, s->lanes), rl = sph_list_regs(s->arith, s->dim, -1);
   if (rp <= 0 || rl <= 0) return PG_OK;
@@ -523,13 +569,7 @@ int choose_overlap(pg_system* s, int sms) {
   int bl = (regs - bp * per_block_p) / per_block_l;
   bl = std::min(bl, (threads - bp * s->block) / s->block);
   if (bl < 1) return PG_OK;
-  if (!s->aux) {  // the list kernel's blocks are placed first, the continuity pass fills the rest
-    int least = 0, greatest = 0;
-    PG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-    PG_CUDA_TRY(cudaStreamCreateWithPriority(&s->aux, cudaStreamNonBlocking, greatest));
-  }
-  for (int i = 0; i < 2; ++i)
-    if (!s->ov_ev[i]) PG_CUDA_TRY(cudaEventCreateWithFlags(&s->ov_ev[i], cudaEventDisableTiming));
+  PG_TRY(ensure_aux_stream(s));
   // the continuity pass beside the lists runs one block per tile, so the block scheduler fills
   // the SMs with it as the list kernel's blocks finish
   s->ov_pass_grid = 0;

@@ -110,7 +110,9 @@ int launch_sph_list_pf(cudaStream_t st, const SphArgs& a, int pf_index, int grid
 // part 0 and 1 the continuity pass (pair values, then the sums, rho' and the {rho', P'} pack),
 // part 2 and 3 the momentum pass (pair values, then the sums and the update).  a.fcache holds
 // sph_sym_entry_bytes() per list entry.
-int launch_sph_sym(cudaStream_t st, const SphArgs& a, int part, int block);
+// split > 0 (part 0 only): the lists of the slots from split on may still be being built; the
+// launch with second == 0 takes the slots whose partners all lie below split, second == 1 the rest.
+int launch_sph_sym(cudaStream_t st, const SphArgs& a, int part, int block, uint32_t split = 0, int second = 0);
 size_t sph_sym_entry_bytes();
 
 // Adjoint of one SPH step (pg_adjoint.cu).  s[0..4] hold the slot-ordered packs written by

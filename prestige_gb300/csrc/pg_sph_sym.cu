@@ -178,16 +178,24 @@ __device__ __forceinline__ bool slot_of(const SphArgs& a, Slot& s) {
   return true;
 }
 
+// split > 0: the lists of the slots from split on may still be being built (on another stream).
+// A slot's pair values need its partners' complete lists, so the first launch (second == 0)
+// takes the slots below split whose stored partners all lie below split (lists ascend, so the
+// last stored entry decides) and the second launch, after all lists, the others.
 template <int DIM>
-__global__ void __launch_bounds__(kSphMaxThreads) sym_c1_kernel(SphArgs a) {
+__global__ void __launch_bounds__(kSphMaxThreads) sym_c1_kernel(SphArgs a, uint32_t split, int second) {
   Slot s;
   if (!slot_of(a, s)) return;
+  const uint32_t* __restrict__ my = a.nlist + list_base(s.k, a.cap);
+  if (split) {
+    const bool early = s.k < split && (s.L == 0 || my[(size_t)(s.L - 1) * kListTile] < split);
+    if (early == (second != 0)) return;
+  }
   const SphK& K = a.sys[sys_of_slot(a, s.id)];
   const double4_32a* __restrict__ A = (const double4_32a*)a.s[0];
   const double4_32a* __restrict__ B = (const double4_32a*)a.s[1];
   const Planes P = planes_of(a);
   const double4_32a Ai = A[s.k], Bi = B[s.k];
-  const uint32_t* __restrict__ my = a.nlist + list_base(s.k, a.cap);
   // all lanes at the same entry index, so the entry-plane stores coalesce (starting each lane at
   // its own first upper entry, found by binary search, measured the same)
   for (uint32_t q = 0; q < s.L; ++q) {
@@ -312,7 +320,6 @@ typedef void (*SymKernel)(SphArgs);
 template <int DIM>
 SymKernel sym_kernel(int part) {
   switch (part) {
-    case 0: return sym_c1_kernel<DIM>;
     case 1: return sym_c2_kernel<DIM>;
     case 2: return sym_m1_kernel<DIM>;
     case 3: return sym_m2_kernel<DIM>;
@@ -324,9 +331,9 @@ SymKernel sym_kernel(int part) {
 
 size_t sph_sym_entry_bytes() { return 4 * sizeof(double) + sizeof(uint32_t); }
 
-int launch_sph_sym(cudaStream_t st, const SphArgs& a, int part, int block) {
+int launch_sph_sym(cudaStream_t st, const SphArgs& a, int part, int block, uint32_t split, int second) {
   SymKernel kern = a.dim == 2 ? sym_kernel<2>(part) : sym_kernel<3>(part);
-  if (!kern) {
+  if (!kern && part != 0) {
     set_error("unknown part %d of the pair-once step", part);
     return PG_EINVAL;
   }
@@ -336,7 +343,12 @@ int launch_sph_sym(cudaStream_t st, const SphArgs& a, int part, int block) {
   }
   if (a.k_end <= a.k_begin) return PG_OK;
   const unsigned blocks = (unsigned)((a.k_end - a.k_begin + block - 1) / block);
-  kern<<<blocks, block, 0, st>>>(a);
+  if (part == 0) {
+    if (a.dim == 2) sym_c1_kernel<2><<<blocks, block, 0, st>>>(a, split, second);
+    else sym_c1_kernel<3><<<blocks, block, 0, st>>>(a, split, second);
+  } else {
+    kern<<<blocks, block, 0, st>>>(a);
+  }
   PG_CUDA_TRY(cudaGetLastError());
   return PG_OK;
 }

@@ -49,7 +49,7 @@ def lattice_4m():
 def test_lattice_4m_ieee_bit_exact(pg, oracle, lattice_4m):
     w = lattice_4m
     s, cfg = _handle(w, 0)
-    assert s.info()["overlap_split"] == 0  # the IEEE mode keeps the sequential schedule
+    assert s.info()["overlap_split"] > 0  # the lists of three quarters beside the first pair values
     st = _ostate(oracle, w)
     for k in (1, 2):
         s.step(k)
