@@ -230,6 +230,13 @@ long long neighbor_launches(const pg_system* s) { return 1 + 3LL * s->nw.passes 
 // continuity pass (rho' into the canonical density and the sorted pack).  ev (optional): events
 // 0-4 of a step (start, after the neighbour search, after the sorted gather, after the lists,
 // after the continuity pass).
+// The IEEE f64 step evaluates each pair once (pg_sph_sym.cu: four kernels) from 16,384 particles;
+// below, where the step is bound by the latency of its launches, the two-sided passes (two
+// kernels) are faster: the 6,518-particle dam break took 0.149 against 0.125 ms per step.  Both
+// give the oracle's bits.
+constexpr size_t kPairOnceMin = 16384;
+bool pair_once(const pg_system* s) { return s->arith == ARITH_F64_EXACT && s->n >= kPairOnceMin; }
+
 int enqueue_sph_front(pg_system* s, cudaEvent_t* ev) {
   if (ev) PG_CUDA_TRY(cudaEventRecord(ev[0], s->stream));
   PG_TRY(enqueue_neighbors(s));
@@ -259,7 +266,7 @@ int enqueue_sph_front(pg_system* s, cudaEvent_t* ev) {
     s->launches += neighbor_launches(s) + 6;
     return PG_OK;
   }
-  if (s->arith == ARITH_F64_EXACT) {
+  if (pair_once(s)) {
     // each pair once (pg_sph_sym.cu): the pair values of a slot need its partners' complete lists
     PG_TRY(launch_sph_list(s->stream, a, s->arith, s->list_grid, s->block));
     s->list_arith = s->arith;
@@ -305,7 +312,7 @@ int enqueue_sph_front(pg_system* s, cudaEvent_t* ev) {
 // update).  ev (optional): event 5 of a step (end).
 int enqueue_sph_momentum(pg_system* s, cudaEvent_t* ev) {
   SphArgs a = sph_args(s, 1, false);
-  if (s->arith == ARITH_F64_EXACT) {
+  if (pair_once(s)) {
     PG_TRY(launch_sph_sym(s->stream, a, 2, mom_block(s)));
     PG_TRY(launch_sph_sym(s->stream, a, 3, mom_block(s)));
     s->launches += 2;

@@ -307,3 +307,34 @@ def test_ieee_overlapped_lists_match_the_oracle_bit_exact(pg, oracle, cap):
     g.enable_graph(True)
     g.step(1)
     assert np.array_equal(g.get("pos"), s.get("pos")) and np.array_equal(g.get("rho"), s.get("rho"))
+
+
+@pytest.mark.parametrize("cap", [4, 16, 48, 128])
+def test_pair_once_ieee_bit_exact(pg, oracle, cap):
+    """The IEEE step evaluates each pair once from 16,384 particles (below, the two-sided passes
+    run).  3D lattice of 20,000 particles, bit-exact with the oracle over two steps, with lists
+    cut at 4, 16 or 48 entries (about 74 neighbours: pairs held by one list only, continued
+    walks) and with full lists."""
+    w = workloads.sph_lattice_3d(n=20000, seed=23)
+    cfg = dict(w["config"])
+    cfg.update(precision=1, f64_mode=0, list_capacity=cap)
+    s = ParticleSystem(make_config(**cfg), w["n"])
+    workloads.load_into(s, w)
+    st = _ostate(oracle, w)
+    s.step(2)
+    oracle.sph_run(cfg, st, 2)
+    assert np.array_equal(s.get("pos"), st.pos) and np.array_equal(s.get("rho"), st.rho)
+    assert np.array_equal(s.get("vel"), st.vel)
+
+
+def test_pair_once_ieee_2d_dam_break_bit_exact(pg, oracle):
+    """The pair-once IEEE kernels in 2D with walls: the dam break at dx = 0.01 (20,000 fluid
+    particles and the wall layers), bit-exact with the oracle over three steps."""
+    w = workloads.dam_break_2d(dx=0.01)
+    assert w["n"] >= 16384
+    s, cfg = _pair(w, 1, 0)
+    st = _ostate(oracle, w)
+    s.step(3)
+    oracle.sph_run(cfg, st, 3)
+    assert np.array_equal(s.get("pos"), st.pos) and np.array_equal(s.get("rho"), st.rho)
+    assert np.array_equal(s.get("vel"), st.vel)
