@@ -23,10 +23,12 @@
 //   dLam_M/dv = -F c1 xE x,   dLam_M/drho_i = -F xE (P'(rho_i) - Pi / (rho_i + rho_j)),
 //   dLam_C/dx = G w D x + F D v,   dLam_C/dv = F D x
 // with xE = x . E and P'(rho) = B ((gamma - 2)(rho/rho0)^gamma + 2) / rho^3 (all densities
-// are rho', the ones the momentum rate used).  Each thread evaluates Lam for all its
-// neighbours, so the transpose of the pair Jacobian is a second gather over the same cell
-// lists (no atomics, deterministic order).  The parameter derivatives are the derivatives of
-// Lam_M per unordered pair, each thread taking half of every pair it sees:
+// are rho', the ones the momentum rate used).  The mixed-precision adjoint (below) evaluates Lam
+// for all of a thread's neighbours, so the transpose of the pair Jacobian is a second gather
+// over the same cell lists (no atomics, deterministic order); the FP64 adjoint
+// (pg_adjoint_sym.cu) evaluates each pair once and writes the partner's share, the negated
+// vectors, into the partner's list entry.  The parameter derivatives are the derivatives of
+// Lam_M per unordered pair, each side taking half of every pair it evaluates:
 //   dPhi/dalpha += -1/2 F xE (-2 c0 h) w / ((r^2 + eps h^2)(rho_i + rho_j))   (w < 0)
 //   dPhi/dB     += -1/2 F xE (P_i + P_j) / B
 // In this form the cancellation between the two ordered terms is done analytically inside E;
@@ -145,142 +147,6 @@ __global__ void adjoint_prep_kernel(SphArgs a) {
   ((double4_32a*)a.s[3])[k] = make_double4_32a(ab[0], ab[1], ab[2], 0.0);
   ((float4*)a.s[4])[k] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
 }
-
-// STAGE SPH_MOM: adjoint of the momentum rate (seeds abar); also writes dbar = dt lr'_tot into
-// the slot pack DB for the continuity adjoint.  STAGE SPH_CONT: adjoint of the continuity rate.
-template <int DIM, int STAGE>
-struct AdjPairs {
-  static constexpr bool kMom = STAGE == SPH_MOM;
-  const double4_32a *X, *V, *Q, *A;
-  const double* DBp;
-  double fa, fb, inv_h, four_h2, eps_h2, avk, avk_alpha;
-  double xi[3], vi[3], ai[3], rhoi, mi, Pi, Pdi, PBi, dbi;
-  double gx[3], gv[3], gr, gal, gB;
-
-  __device__ __forceinline__ void begin(const SphArgs& a, const SphK& K, uint32_t k) {
-    X = (const double4_32a*)a.s[0];
-    V = (const double4_32a*)a.s[1];
-    Q = (const double4_32a*)a.s[2];
-    A = (const double4_32a*)a.s[3];
-    DBp = (const double*)a.s[5];
-    fa = K.d.fa;
-    fb = K.d.fb;
-    inv_h = K.d.inv_h;
-    four_h2 = K.d.four_h2;
-    eps_h2 = K.d.eps_h2;
-    avk = K.d.avk;
-    avk_alpha = K.avk_alpha;
-    const double4_32a x = X[k], v = V[k];
-    xi[0] = x.x; xi[1] = x.y; xi[2] = x.z; mi = x.w;
-    vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; rhoi = v.w;
-    Pi = Pdi = PBi = dbi = 0.0;
-    ai[0] = ai[1] = ai[2] = 0.0;
-    if (kMom) {
-      const double4_32a q = Q[k], ab = A[k];
-      Pi = q.x; Pdi = q.y; PBi = q.z;
-      ai[0] = ab.x; ai[1] = ab.y; ai[2] = ab.z;
-    } else {
-      dbi = DBp[k];
-    }
-    gx[0] = gx[1] = gx[2] = 0.0;
-    gv[0] = gv[1] = gv[2] = 0.0;
-    gr = gal = gB = 0.0;
-  }
-
-  __device__ __forceinline__ void pair(uint32_t t) {
-    const double4_32a xj = X[t];
-    double d[3] = {xi[0] - xj.x, xi[1] - xj.y, DIM == 3 ? xi[2] - xj.z : 0.0};
-    // the forward pass's neighbour test, same operation order
-    double r2 = __dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1]));
-    if (DIM == 3) r2 = __dadd_rn(r2, __dmul_rn(d[2], d[2]));
-    if (!(r2 < four_h2) || !(r2 > 0.0)) return;
-    const double4_32a vj = V[t];
-    const double mj = xj.w;
-    const double r = sqrt(r2);
-    const double inv_r = 1.0 / r;
-    const double q = r * inv_h;
-    double F, G;
-    if (q < 1.0) {
-      F = fa * (2.25 * q - 3.0);
-      G = fa * 2.25 * inv_h * inv_r;
-    } else {
-      const double tq = 2.0 - q;
-      F = fb * tq * tq * inv_r;
-      G = -(fb * tq * inv_r) * (2.0 * inv_h + tq * inv_r) * inv_r;
-    }
-    const double dv[3] = {vi[0] - vj.x, vi[1] - vj.y, DIM == 3 ? vi[2] - vj.z : 0.0};
-    double w = dv[0] * d[0] + dv[1] * d[1];
-    if (DIM == 3) w += dv[2] * d[2];
-    if (!kMom) {
-      const double D = dbi * mj + DBp[t] * mi;
-      const double gw = G * w * D, fd = F * D;
-#pragma unroll
-      for (int c = 0; c < DIM; ++c) {
-        gx[c] += gw * d[c] + fd * dv[c];
-        gv[c] += fd * d[c];
-      }
-      return;
-    }
-    const double4_32a qj = Q[t], aj = A[t];
-    const double rb = rhoi + vj.w;
-    const double e = r2 + eps_h2;
-    double c1 = 0.0, c1a = 0.0;
-    if (w < 0.0) {
-      const double base = 1.0 / (e * rb);
-      c1 = avk * base;
-      c1a = avk_alpha * base;
-    }
-    const double PI = c1 * w;
-    const double S = Pi + qj.x + PI;
-    double E[3], xE = 0.0;
-#pragma unroll
-    for (int c = 0; c < DIM; ++c) {
-      E[c] = mj * ai[c] - mi * (c == 0 ? aj.x : c == 1 ? aj.y : aj.z);
-      xE += d[c] * E[c];
-    }
-    const double a1 = -G * S * xE + 2.0 * F * xE * PI / e;
-    const double b1 = -F * c1 * xE;
-    const double fs = F * S;
-#pragma unroll
-    for (int c = 0; c < DIM; ++c) {
-      gx[c] += a1 * d[c] + b1 * dv[c] - fs * E[c];
-      gv[c] += b1 * d[c];
-    }
-    gr -= F * xE * (Pdi - PI / rb);
-    const double half = 0.5 * F * xE;
-    gal -= half * c1a * w;
-    gB -= half * (PBi + qj.z);
-  }
-
-  __device__ __forceinline__ void finish(const SphArgs& a, const SphK& K, uint32_t id, uint32_t k) {
-    double* lx = (double*)a.lam[0];
-    double* lv = (double*)a.lam[1];
-    double* lr = (double*)a.lam[2];
-    if (!kMom) {
-#pragma unroll
-      for (int c = 0; c < DIM; ++c) {
-        const size_t o = (size_t)id * DIM + c;
-        lx[o] += gx[c];
-        lv[o] += gv[c];
-      }
-      return;
-    }
-    const bool fluid = id < K.fluid_end;
-    const double dt = K.d.dt;
-#pragma unroll
-    for (int c = 0; c < DIM; ++c) {
-      const size_t o = (size_t)id * DIM + c;
-      const double lxo = lx[o];
-      lx[o] = lxo + gx[c];
-      lv[o] = (fluid ? lv[o] + dt * lxo : lv[o]) + gv[c];
-    }
-    const double lrt = lr[id] + gr;
-    lr[id] = lrt;
-    ((double*)a.s[5])[k] = dt * lrt;
-    ((double*)a.lam[3])[id] += gal;
-    ((double*)a.lam[4])[id] += gB;
-  }
-};
 
 // ---------------------------------------------------------------------------------------
 // Mixed-precision adjoint (handles in the fast f64 mode).  Positions and velocities are packed
@@ -560,17 +426,17 @@ int launch_adjoint_prep(cudaStream_t st, const SphArgs& a, bool fp32) {
 
 typedef void (*AdjKernel)(SphArgs, int);
 
+// The two-sided passes of the mixed-precision adjoint (the FP64 adjoint evaluates each pair once:
+// pg_adjoint_sym.cu).
 template <int DIM>
-AdjKernel adjoint_kernel_dim(int stage, bool fp32) {
-  if (fp32)
-    return stage == SPH_MOM ? sph_list_pass_kernel<AdjPairsF<DIM, SPH_MOM>, DIM, false>
-                            : sph_list_pass_kernel<AdjPairsF<DIM, SPH_CONT>, DIM, false>;
-  return stage == SPH_MOM ? sph_list_pass_kernel<AdjPairs<DIM, SPH_MOM>, DIM, false>
-                          : sph_list_pass_kernel<AdjPairs<DIM, SPH_CONT>, DIM, false>;
+AdjKernel adjoint_kernel_dim(int stage) {
+  return stage == SPH_MOM ? sph_list_pass_kernel<AdjPairsF<DIM, SPH_MOM>, DIM, false>
+                          : sph_list_pass_kernel<AdjPairsF<DIM, SPH_CONT>, DIM, false>;
 }
 
 AdjKernel adjoint_kernel(int dim, int stage, bool fp32) {
-  return dim == 2 ? adjoint_kernel_dim<2>(stage, fp32) : adjoint_kernel_dim<3>(stage, fp32);
+  if (!fp32) return nullptr;
+  return dim == 2 ? adjoint_kernel_dim<2>(stage) : adjoint_kernel_dim<3>(stage);
 }
 
 // Prefilter positions (float4 x, y, z) of the list kernel and of overflow walks: the FP64 packs
@@ -578,6 +444,10 @@ AdjKernel adjoint_kernel(int dim, int stage, bool fp32) {
 int adjoint_pf_index(bool fp32) { return fp32 ? 0 : 4; }
 
 int launch_adjoint_pass(cudaStream_t st, const SphArgs& a, int stage, int grid, bool fp32) {
+  if (!fp32) {
+    set_error("the FP64 adjoint runs the pair-once kernels");
+    return PG_EINVAL;
+  }
   if (a.n == 0) return PG_OK;
   const uint32_t ntiles = (a.n + kSphThreads - 1) / kSphThreads;
   if (grid <= 0 || (uint32_t)grid > ntiles) grid = (int)ntiles;
@@ -587,9 +457,10 @@ int launch_adjoint_pass(cudaStream_t st, const SphArgs& a, int stage, int grid, 
 }
 
 int adjoint_pass_occupancy(int dim, int stage, bool fp32) {
+  AdjKernel kern = adjoint_kernel(dim, stage, fp32);
   int blocks = 0;
-  cudaError_t e =
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, adjoint_kernel(dim, stage, fp32), kSphThreads, 0);
+  if (!kern) return 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, kSphThreads, 0);
   return e == cudaSuccess ? blocks : 0;
 }
 
@@ -708,7 +579,7 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
   PG_TRY(A->A4.ensure(32 * (nn + pg::kPackPad)));
   PG_TRY(A->PF.ensure(16 * (nn + pg::kPackPad)));
   PG_TRY(A->DB.ensure(8 * (nn + pg::kPackPad)));
-  if (A->pass_grid_fp32 != (int)fp32 || A->pass_grid[pg::SPH_MOM] == 0) {
+  if (fp32 && (A->pass_grid_fp32 != (int)fp32 || A->pass_grid[pg::SPH_MOM] == 0)) {
     int dev = 0, sms = 0;
     PG_CUDA_TRY(cudaGetDevice(&dev));
     PG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

@@ -359,7 +359,8 @@ __global__ void __launch_bounds__(kSphMaxThreads) adj_a2_kernel(SphArgs a) {
   if (s.overflow)
     resume_walk<DIM>(a, K, P, s.k, xk,
                      [&](uint32_t t) { add_own<DIM>(sum, mom_terms<DIM>(K, P, s.k, t, xk, vk), Pdk, 0.5); });
-  // the momentum adjoint's update (two-sided form: AdjPairs<DIM, SPH_MOM>::finish)
+  // the momentum adjoint's update: lx += gx, lv += dt lx' (fluid) + gv, lr += gr, dbar = dt lr for
+  // the continuity pass, and the parameter sums
   double* lx = (double*)a.lam[0];
   double* lv = (double*)a.lam[1];
   double* lr = (double*)a.lam[2];
