@@ -6,7 +6,7 @@ References
     directional derivative <dL/dv0, u> for a seeded direction u): the FP64 adjoint (IEEE handles)
     agrees to 1e-8 (measured on a GB300: 6e-15, 3e-14 and 1e-14 at full size), the
     mixed-precision adjoint (double-word handles) to 1e-5 for dL/dalpha and <dL/dv0, u>
-    (measured 1.3e-7 and 5.6e-7) and to 5e-5 for dL/dB (measured 1.3e-5 to 1.7e-5: its pair
+    (measured 1.3e-7 and 2.7e-8) and to 5e-5 for dL/dB (measured 1.3e-5 to 1.7e-5: its pair
     terms are about 1e3 times its total, which amplifies the FP32 floor of the pair
     derivatives);
   * central finite differences of the IEEE forward run: dL/dalpha at eps = 1e-6 to 1e-5 for both
