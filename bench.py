@@ -647,7 +647,7 @@ def run_gpu(args, rank, world, local, pgroup):
                   "particles_per_warp": s.info()["particles_per_warp"], "cell_multiplier": args.cell_mult,
                   "fixed": True}
     elif not args.no_autotune:  # outside the timed region; the state is restored by the tuner
-        tuning = s.autotune(trial_steps=8)
+        tuning = s.autotune(trial_steps=16)  # 8-step trials picked block sizes 1-2 % off on some boxes
     info = s.info()
     from prestige_gb300._native import measure_fma_peaks
     fp64_peak, fp32_peak = measure_fma_peaks()  # ~10 ms of FMA chains, before the timed region
