@@ -231,11 +231,30 @@ __global__ void __launch_bounds__(kSphMaxThreads) sym_c2_kernel(SphArgs a) {
     pair_geometry<DIM>(c, Ai, Bi, A[t], B[t], d, r2, F, w);
     return D::mul(w, F);
   };
+  // software pipeline: list entries two ahead, the partner's mass and list length and the
+  // entry's stored value one ahead (the pass waits on these loads; its FP64 work is two
+  // operations per entry, summed in list order)
   double dr = 0.0;
-  for (uint32_t q = 0; q < s.L; ++q) {
-    const uint32_t t = my[(size_t)q * kListTile];
-    const double wF = t > s.k || holds(a, t, s.k) ? *P.S(entry(s.k, q, a.cap)) : full(t);
-    dr = D::add(dr, D::mul(A[t].w, wF));
+  const uint32_t L = s.L;
+  uint32_t t = L > 0 ? my[0] : 0u;
+  uint32_t tn = L > 1 ? my[kListTile] : 0u;
+  double mt = L > 0 ? A[t].w : 0.0;
+  uint32_t nl = L > 0 ? a.nlen[t] : 0u;
+  double sv = L > 0 ? *P.S(entry(s.k, 0, a.cap)) : 0.0;
+  for (uint32_t q = 0; q < L; ++q) {
+    const uint32_t tnn = q + 2 < L ? my[(size_t)(q + 2) * kListTile] : 0u;
+    const double mtn = q + 1 < L ? A[tn].w : 0.0;
+    const uint32_t nln = q + 1 < L ? a.nlen[tn] : 0u;
+    const double svn = q + 1 < L ? *P.S(entry(s.k, q + 1, a.cap)) : 0.0;
+    // the value is in the entry unless the partner below is one whose list did not reach this
+    // slot (holds())
+    const bool stored = t > s.k || nl <= a.cap || a.nlist[entry(t, a.cap - 1, a.cap)] >= s.k;
+    dr = D::add(dr, D::mul(mt, stored ? sv : full(t)));
+    t = tn;
+    tn = tnn;
+    mt = mtn;
+    nl = nln;
+    sv = svn;
   }
   if (s.overflow) resume_walk<DIM>(a, K, s.k, Ai, [&](uint32_t t) { dr = D::add(dr, D::mul(A[t].w, full(t))); });
   double* rho = (double*)a.rho;
