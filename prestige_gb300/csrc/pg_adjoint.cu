@@ -494,6 +494,50 @@ int check_differentiable(pg_system* s) {
 
 }  // namespace pg
 
+namespace {
+
+// The double-word recompute of an IEEE handle's backward pass: enter() switches the handle to
+// the double-word mode (the same cell multiplier and block size), leave() restores the IEEE
+// mode, the momentum block, the particles per warp and a captured graph.  The destructor
+// restores the mode after an early error return.
+struct RecomputeMode {
+  pg_system* s;
+  bool active;
+  bool switched = false;
+  double mult = 1.0;
+  int block = 0, mom = 0, lanes = 1;
+  bool graph = false;
+  RecomputeMode(pg_system* sys, bool act) : s(sys), active(act) {}
+  int enter() {
+    if (!active) return PG_OK;
+    mult = s->cfg.cell_multiplier;
+    block = s->block;
+    mom = s->block_mom;
+    lanes = s->lanes;
+    graph = s->graph_enabled;
+    s->graph_enabled = false;
+    switched = true;
+    return pg::retune_sph(s, mult, PG_F64_FAST, block);
+  }
+  int leave() {
+    if (!switched) return PG_OK;
+    switched = false;
+    PG_TRY(pg::retune_sph(s, mult, PG_F64_NATIVE, block));
+    PG_TRY(pg::set_momentum_block(s, mom));
+    PG_TRY(pg::set_pass_lanes(s, lanes));
+    if (graph) {
+      PG_TRY(pg::capture_graphs(s));
+      s->graph_enabled = true;
+    }
+    return PG_OK;
+  }
+  ~RecomputeMode() {
+    if (switched) leave();
+  }
+};
+
+}  // namespace
+
 extern "C" {
 
 int pg_forward_checkpointed(pg_system* s, int nsteps, int every) {
@@ -548,6 +592,15 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
   const size_t n = s->n, nn = n ? n : 1, nd = n * (size_t)s->dim;
   const size_t ncp1 = s->ncells + 1;
   const int every = A->every;
+  // fast f64 handles: mixed-precision adjoint pair terms; IEEE handles: FP64
+  const bool fp32 = s->arith == pg::ARITH_F64_DF;
+  // An IEEE handle recomputes its segments in the double-word mode (FP32 pipe), from the IEEE
+  // checkpoints of the forward run: the recompute then hardly competes with the FP64 adjoint
+  // sweep that runs beside it.  Over one segment the recomputed states stay within about 1e-12
+  // of the IEEE trajectory (the double-word drift bound), far inside the adjoint's accuracy
+  // against the dual-number gradient.  The handle's mode and schedule are restored at the end.
+  RecomputeMode mode_guard(s, !fp32);
+  PG_TRY(mode_guard.enter());
   for (int b = 0; b < 2; ++b) {
     PG_TRY(A->seg_state[b].ensure(8 * A->state_doubles * every + 8));
     PG_TRY(A->seg_rnext[b].ensure(8 * nn * every));
@@ -571,8 +624,6 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
   PG_TRY(A->lr.ensure(8 * nn));
   PG_TRY(A->ga.ensure(8 * nn));
   PG_TRY(A->gb.ensure(8 * nn));
-  // fast f64 handles: mixed-precision adjoint pair terms; IEEE handles: FP64
-  const bool fp32 = s->arith == pg::ARITH_F64_DF;
   PG_TRY(A->X4.ensure(32 * (nn + pg::kPackPad)));
   PG_TRY(A->V4.ensure(32 * (nn + pg::kPackPad)));
   PG_TRY(A->Q4.ensure(32 * (nn + pg::kPackPad)));
@@ -699,6 +750,7 @@ int pg_backward(pg_system* s, const double* dL_dx, double* dL_dalpha, double* dL
   }
   PG_TRY(pg::sync_and_check(s));
   s->nbr_valid = false;
+  PG_TRY(mode_guard.leave());
   // fixed-order pairwise sums of the per-particle partials
   auto tree_sum = [](std::vector<double>& v) {
     size_t m = v.size();

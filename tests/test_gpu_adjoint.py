@@ -7,8 +7,10 @@ Checks
   * against the oracle's forward-mode dual-number gradient (same loss, same steps): relative
     1e-8 for the FP64 adjoint and 1e-5 for the mixed-precision one, for dL/dalpha, dL/dB and
     the directional derivative <dL/dv0, u>;
-  * the checkpoint interval does not change the result (bit for bit), and the handle's state
-    after pg_backward is the final forward state.
+  * the checkpoint interval does not change the result (bit for bit for the double-word handle;
+    within 1e-11 for the IEEE handle, whose segments are recomputed in the double-word mode), the
+    handle's state after pg_backward is the final forward state, and the handle steps in its own
+    mode and schedule afterwards.
 Loss: L = mean over fluid particles of |x_i(T) - target_i|^2, so dL/dx_i = 2 (x_i - t_i) / n_fluid.
 """
 import numpy as np
@@ -149,13 +151,45 @@ def test_adjoint_with_lists_cut_short_matches_dual_numbers(pg, oracle, mode, cap
     _dual_check(oracle, _small_3d(), nsteps=8, every=3, mode=mode, list_capacity=cap)
 
 
-def test_checkpoint_interval_does_not_change_gradients(pg):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_checkpoint_interval_does_not_change_gradients(pg, mode):
+    """The double-word handle recomputes its segments in its own mode, so the checkpoint interval
+    changes nothing, bit for bit.  The IEEE handle recomputes each segment in the double-word
+    mode from the segment's IEEE checkpoint, so the states it linearises about depend on where
+    the segment starts, within the double-word drift (about 1e-12): the gradients agree to 1e-11."""
     w = _small_3d()
-    ref = _gradients(w, 9, 9)
+    ref = _gradients(w, 9, 9, f64_mode=mode)
     for every in (1, 4):
-        got = _gradients(w, 9, every)
-        assert got[0] == ref[0] and got[1] == ref[1]
-        assert np.array_equal(got[2], ref[2])
+        got = _gradients(w, 9, every, f64_mode=mode)
+        if mode == 1:
+            assert got[0] == ref[0] and got[1] == ref[1]
+            assert np.array_equal(got[2], ref[2])
+        else:
+            assert abs(got[0] - ref[0]) <= 1e-11 * abs(ref[0])
+            assert abs(got[1] - ref[1]) <= 1e-11 * abs(ref[1])
+            assert np.abs(got[2] - ref[2]).max() <= 1e-11 * np.abs(ref[2]).max()
+
+
+def test_backward_restores_the_handle(pg):
+    """pg_backward on an IEEE handle switches to the double-word mode for its recompute and back:
+    afterwards the handle steps in the IEEE mode with its block sizes and graph, bit for bit as
+    a handle that never ran the backward pass."""
+    w = _small_3d()
+    a, _ = _system(w)
+    a.set_momentum_block(128)
+    a.enable_graph(True)
+    a.forward_checkpointed(4, 2)
+    x = a.get("pos")
+    a.backward(_dloss(w, x))
+    info = a.info()
+    assert info["arith"] == 0 and info["momentum_block"] == 128
+    b, _ = _system(w)
+    b.step(4)
+    a.step(3)
+    b.step(3)
+    assert np.array_equal(a.get("pos"), b.get("pos")) and np.array_equal(a.get("rho"), b.get("rho"))
+    a.close()
+    b.close()
 
 
 def test_backward_needs_forward(pg):
