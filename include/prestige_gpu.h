@@ -255,8 +255,11 @@ int pg_dem_set_history(pg_system* sys, const uint32_t* partner, const double* xi
 /* Differentiable SPH (f64, single system).  pg_forward_checkpointed runs nsteps from the current
  * state, keeping the state every `every` steps.  pg_backward then takes dL/dx of the final
  * positions (n*dim, id order) and returns dL/dalpha, dL/dB and dL/dv0 (n*dim, id order); any
- * output pointer may be NULL.  The handle's state stays the final state.  No reference
- * counterpart (the reference has no differentiation). */
+ * output pointer may be NULL.  The handle's state stays the final state.  An IEEE handle
+ * recomputes each segment from its IEEE checkpoint in the double-word mode (within about 1e-12 of
+ * the IEEE trajectory over a segment) and evaluates the adjoint in FP64; its mode, block sizes and
+ * graph are restored before the call returns.  No reference counterpart (the reference has no
+ * differentiation). */
 int pg_forward_checkpointed(pg_system* sys, int nsteps, int every);
 int pg_backward(pg_system* sys, const double* dL_dx, double* dL_dalpha, double* dL_dB, double* dL_dv0);
 

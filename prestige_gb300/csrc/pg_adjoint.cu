@@ -41,7 +41,8 @@
 // (sorted cells, sorted ids, cell table: integer data, reused as is), then sweeps the adjoint
 // back through the segment.  The recompute of the previous segment runs beside the sweep (the
 // handle's stream and a second one), so two segments are held.  Memory: (nsteps / every)
-// checkpoints plus two segments.
+// checkpoints plus two segments.  An IEEE handle recomputes in the double-word mode (see
+// RecomputeMode below).
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
