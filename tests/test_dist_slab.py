@@ -210,3 +210,34 @@ def test_dem_slabs_reproduce_the_single_domain_run(oracle, tmp_path, world):
         with open(out + ".r%d" % r, "rb") as fh:
             owned.append(pickle.load(fh)["owned"])
     assert any(len(set(x)) > 1 for x in owned)  # spheres crossed cuts during the run
+
+
+def test_dem_history_translation_round_trip():
+    """SlabDEM's history helpers: global partner ids to local ids (partners absent from the local
+    system dropped, the order of the rest kept, walls and the empty tail untouched) and back."""
+    sys.path.insert(0, ROOT)
+    from prestige_gb300.slab import NO_PARTNER, WALL_ID, SlabDEM
+
+    class Bare(SlabDEM):
+        def __init__(self, hpid, hxi):  # only the history state
+            self.hpid = np.asarray(hpid, np.uint32)
+            self.hxi = np.asarray(hxi, np.float64)
+
+    E = NO_PARTNER
+    hpid = [[7, 3, WALL_ID + 2, 9, E, E],
+            [5, E, E, E, E, E],
+            [E, E, E, E, E, E]]
+    hxi = np.arange(3 * 6 * 3, dtype=np.float64).reshape(3, 6, 3) + 1.0
+    s = Bare(hpid, hxi)
+    gid_local = np.array([2, 3, 5, 7, 11])          # global id of each local particle
+    g2l = np.full(12, -1, np.int64)
+    g2l[gid_local] = np.arange(gid_local.size)
+    lp, lx = s._history_to_local(g2l)
+    # row 0: 7 -> 3, 3 -> 1, the wall kept, 9 (absent) dropped; its spring goes with it
+    assert lp[0].tolist() == [3, 1, WALL_ID + 2, E, E, E]
+    assert np.array_equal(lx[0, :3], hxi[0, :3]) and not lx[0, 3:].any()
+    assert lp[1].tolist() == [2, E, E, E, E, E] and np.array_equal(lx[1, 0], hxi[1, 0])
+    assert (lp[2] == E).all() and not lx[2].any()
+    back = SlabDEM._history_to_global(lp, gid_local)
+    assert back[0].tolist() == [7, 3, WALL_ID + 2, E, E, E]
+    assert back[1].tolist() == [5, E, E, E, E, E]
