@@ -83,7 +83,7 @@ SphK make_sphk(const pg_config& c, const Grid& g, uint32_t cell_base, uint32_t i
   df_split(-4.0 * fb / h, &k.w.far0[0], &k.w.far0[1]);
   df_split(fb / (h * h), &k.w.far1[0], &k.w.far1[1]);
   df_split(4.0 * fb, &k.w.far2[0], &k.w.far2[1]);
-  k.w.h = (float)h;
+  k.w.h2 = (float)(h * h);
   k.w.band = (float)(1e-9 * k.d.four_h2);
   k.two_h_f = (float)(2.0 * h) * 1.0000001f;
   k.pos_pad = 8.0 * h;

@@ -43,7 +43,7 @@ struct SphDF {
   // 1 <= q < 2 (far), with q = r/h:  near c0 = -3 fa, c1 = 2.25 fa/h;  far c0 = -4 fb/h,
   // c1 = fb/h^2, c2 = 4 fb
   float near0[2], near1[2], far0[2], far1[2], far2[2];
-  float h;
+  float h2;  // h^2: r^2 < h^2 selects the near piece
   float band;  // |r^2 - (2h)^2| below which the exact f64 test decides
 };
 

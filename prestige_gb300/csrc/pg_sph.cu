@@ -405,13 +405,14 @@ struct DfPairs {
       F = df_make(p.fw.x, p.fw.y);
     } else {
       const df inv_r = df_rsqrt(r2);
-      const df r = df_mul(r2, inv_r);
-      // F = c0 + c1 r + c2 / r on either piece of the spline, without a branch
-      const bool near = r.hi < w.h;
+      // F = c0 + c1 r + c2 / r = c0 + (c1 r^2 + c2) / r on either piece of the spline, without a
+      // branch and without forming r (F is continuous at r = h, so the piece chosen by the FP32
+      // r^2 there does not matter beyond rounding)
+      const bool near = r2.hi < w.h2;
       const df c0 = near ? df_make(w.near0[0], w.near0[1]) : df_make(w.far0[0], w.far0[1]);
       const df c1 = near ? df_make(w.near1[0], w.near1[1]) : df_make(w.far1[0], w.far1[1]);
       const df c2 = near ? df_make(0.f, 0.f) : df_make(w.far2[0], w.far2[1]);
-      F = df_add_raw(df_add_raw(c0, df_mul(c1, r)), df_mul(c2, inv_r));  // consumed by products
+      F = df_add_raw(c0, df_mul(df_add_raw(df_mul(c1, r2), c2), inv_r));  // consumed by products
     }
     if (CACHED) {
       wv = df_make(p.fw.z, p.fw.w);
