@@ -29,7 +29,7 @@
 //                     the double-word remainder x - q1*y (Karp & Markstein 1997): the correction
 //                     leaves a relative error of about t's error squared, below 2^-44
 //   df_rsqrt          one Newton correction of the FP32 reciprocal square root, with the
-//                     residual 1 - a*y^2 formed in double-word arithmetic
+//                     residual 1 - a*y^2 (about 2^-22) formed by FMAs to about 2^-46 absolute
 //   df_sumsq3 /       |x|^2 and x.y of 3-vectors: the three hi products by TwoProd, summed by
 //   df_dot3           TwoSum, with every second-order term (product errors, hi*lo cross terms,
 //                     sum errors) collected in one FP32 correction (about 30 operations in place
@@ -209,12 +209,16 @@ __device__ __forceinline__ df df_div(df x, df y) {
   return fast_two_sum(q1, q2);
 }
 
-// 1/sqrt(a) for a > 0.
+// 1/sqrt(a) for a > 0.  The residual e = 1 - a y^2 of the FP32 seed y is about 2^-22, so its
+// leading bits suffice: a.hi y = h + l exactly (TwoProd), h y - 1 by one FMA (absolute error
+// about 2^-46), the small terms l y and a.lo y^2 in FP32.  Then y + y e / 2 (Newton).
 __device__ __forceinline__ df df_rsqrt(df a) {
   const float y = rsqrtf(a.hi);
-  const df ay2 = df_mul(a, two_prod(y, y));
-  const df e = df_add_f(df_neg(ay2), 1.0f);  // 1 - a*y^2, small
-  return fast_two_sum(y, __fmul_rn(__fmul_rn(y, e.hi), 0.5f));
+  const float h = __fmul_rn(a.hi, y);
+  const float l = __fmaf_rn(a.hi, y, -h);
+  const float r = __fmaf_rn(h, y, -1.0f);
+  const float e = -__fmaf_rn(__fmaf_rn(a.lo, y, l), y, r);
+  return fast_two_sum(y, __fmul_rn(__fmul_rn(y, e), 0.5f));
 }
 
 // |a|^2 of the vector (a0, a1, a2); pass a zero for a2 in 2D.
